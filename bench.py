@@ -1,0 +1,346 @@
+"""Benchmark: closest-hit rays/s on the 1M-triangle heightfield.
+
+Workload (the configuration the headline metric is quoted on): a
+708x708-vertex heightfield (999,698 triangles) plus its 2-triangle area
+light, SAH BVH built with the reference's algorithm, and 2^22 incoherent
+rays (origins uniform in the mesh bounds inflated by 1, directions uniform
+on the sphere).  One step = one closest-hit pass over all 2^22 rays.
+
+  value       device-resident rays/hits, kernel time from CUDA events on
+              the launching stream; L2 flushed (256 MiB write) between steps
+  e2e         the same pass through the C ABI with pinned HOST buffers:
+              host->device copy of the rays, traversal, device->host copy of
+              the hits and the synchronisation are all inside the timed step
+  roofline    algorithmic bytes per launch (32 B per node tested + 48 B per
+              triangle tested + 32 B ray + 16 B hit, counted by the oracle's
+              reference-order traversal on a 2^16-ray sample and scaled)
+              over the measured launch time, against the measured HBM copy
+              bandwidth
+  cpu_baseline  the CPU oracle (a C++ restatement of the reference's
+              BVHAccelerator::intersect) on a bounded ray sample, all host
+              threads
+
+--impl reference times that CPU implementation alone on the same workload.
+Under torchrun each rank traces its own 2^22 rays against a replicated BVH
+(no collective in the data path); value = all ranks' rays / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GPU Mrays/s (1M tris) & p50/p99 render latency vs plain kernel at equal RMSE"
+WORKLOAD = "heightfield-708x708 (999,700 tris, SAH BVH) + 2^22 incoherent rays, closest hit"
+N_RAYS = 1 << 22
+HBM_FALLBACK_GBS = 6800.0
+REASON_BITS = {
+    0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+    0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+    0x100: "display_clock_setting",
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "trace_closest_heightfield.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clocks and throttle reasons while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = "clocks.sm,clocks.max.sm,clocks_event_reasons.active"
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 3:
+                try:
+                    self.samples.append((float(parts[0]), float(parts[1]), int(parts[2], 16)))
+                except ValueError:
+                    pass
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [s[0] for s in self.samples]
+        mx = max(s[1] for s in self.samples)
+        bits = 0
+        for s in self.samples:
+            bits |= s[2]
+        reasons = [name for b, name in REASON_BITS.items() if bits & b and b != 0x1]
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def build_workload(n_rays: int):
+    from pbrt_rust_gb300 import generators as G
+    prims, lights, cam, smp, rays = G.heightfield(n_rays=n_rays)
+    return prims, lights, cam, smp, rays
+
+
+def cpu_rays_per_s(prims, rays, sample: int, nthreads: int):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    ob = O.OracleBVH(prims, 4, "sah")
+    sub = np.ascontiguousarray(rays[:sample])
+    ob.intersect(sub[:1024], nthreads=nthreads)
+    t0 = time.perf_counter()
+    hits, cnt = ob.intersect(sub, nthreads=nthreads, counters=True)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt, cnt, ob
+
+
+def algorithmic_bytes_per_ray(ob, rays, sample: int = 1 << 16):
+    sub = np.ascontiguousarray(rays[:: max(1, len(rays) // sample)][:sample])
+    _, cnt = ob.intersect(sub, counters=True)
+    n = len(sub)
+    nodes, tris = cnt[0] / n, cnt[1] / n
+    return 32.0 * nodes + 48.0 * tris + 32.0 + 16.0, nodes, tris
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    prims, _, _, _, rays = build_workload(N_RAYS)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    ob = O.OracleBVH(prims, 4, "sah")
+    per_step = 1 << 19
+    for i in range(args.warmup):
+        ob.intersect(rays[(i * per_step) % N_RAYS:][:per_step], nthreads=nthreads)
+    times = []
+    for i in range(args.steps):
+        sub = np.ascontiguousarray(rays[(i * per_step) % N_RAYS:][:per_step])
+        t0 = time.perf_counter()
+        ob.intersect(sub, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = per_step / (ms / 1e3) / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample": f"{per_step} rays per step", "threads": nthreads},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{per_step} of the 2^22 rays per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    from pbrt_rust_gb300 import abi
+    from pbrt_rust_gb300.gpu import GpuBVHAccel, GpuSamplerRenderer, GpuScene
+
+    lib = abi.load()
+    prims, lights, cam, smp, rays = build_workload(N_RAYS)
+    t0 = time.perf_counter()
+    bvh = GpuBVHAccel(prims, 4, "sah")
+    build_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream(device=dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    rays_dev = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    hits_dev = torch.empty((N_RAYS, 4), dtype=torch.float32, device=dev)
+    occ_dev = torch.empty((N_RAYS,), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    rp, hp, op = C.c_void_p(rays_dev.data_ptr()), C.c_void_p(hits_dev.data_ptr()), C.c_void_p(occ_dev.data_ptr())
+
+    def closest():
+        abi.check(lib.pbrtgpu_intersect(bvh._h, rp, N_RAYS, hp, sh), lib)
+
+    def anyhit():
+        abi.check(lib.pbrtgpu_intersect_p(bvh._h, rp, N_RAYS, op, sh), lib)
+
+    def timed(fn, steps, warmup):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                flush.zero_()
+                fn()
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        evs = []
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                evs.append((a, b))
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        return [a.elapsed_time(b) for a, b in evs]
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms_closest = timed(closest, args.steps, args.warmup)
+    ms_any = timed(anyhit, max(3, args.steps // 2), args.warmup)
+
+    # e2e: pinned host buffers through the C ABI (copies inside the step)
+    rays_host = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    hits_host = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
+    rh, hh = C.c_void_p(rays_host.data_ptr()), C.c_void_p(hits_host.data_ptr())
+    for _ in range(args.warmup):
+        abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_mrays = N_RAYS / statistics.mean(e2e_t) / 1e6
+    # the host copy of the result must equal the device-resident one
+    torch.cuda.synchronize(dev)
+    if not torch.equal(hits_host, hits_dev.cpu()):
+        raise RuntimeError("host-buffer and device-buffer hits differ")
+
+    # render of the same scene: 1024x1024, 16 spp, direct lighting
+    scene = GpuScene(prims, lights)
+    renderer = GpuSamplerRenderer(smp, cam)
+    img = torch.empty((1024, 1024, 3), dtype=torch.float32, device=dev)
+    renderer.render(scene, out=img, stream=stream)
+    rt = []
+    for _ in range(3):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        renderer.render(scene, out=img, stream=stream)
+        rt.append(time.perf_counter() - t0)
+
+    mean_ms = statistics.mean(ms_closest)
+    t_local = torch.tensor([mean_ms], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t_local, op=torch.distributed.ReduceOp.MAX)
+    ms_step = float(t_local.item())
+    value = ws * N_RAYS / (ms_step / 1e3) / 1e6
+
+    out = None
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        nthreads = os.cpu_count() or 1
+        cpu_sample = 1 << 18
+        cpu_rps, cpu_dt, _, ob = cpu_rays_per_s(prims, rays, cpu_sample, nthreads)
+        bpr, nodes_pr, tris_pr = algorithmic_bytes_per_ray(ob, rays)
+        alg_bytes = bpr * N_RAYS
+        achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+        tr = committed_traffic()
+        out = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "rays_per_step": N_RAYS, "bvh": "reference SAH, 1-prim leaves",
+                       "l2": "flushed between steps (256 MiB write); inputs also exceed L2",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": (tr or {}).get("dram_bytes_per_launch"),
+                         "algorithmic_bytes_per_ray": bpr, "nodes_tested_per_ray": nodes_pr,
+                         "tris_tested_per_ray": tris_pr},
+            "cpu_baseline": {"value": cpu_rps / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+                             "sample": f"first {cpu_sample} of the 2^22 rays, {cpu_dt:.2f} s"},
+            "e2e": {"value": e2e_mrays, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
+                    "d2h_bytes_per_step": N_RAYS * 16},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "any_hit": {"value": N_RAYS / (statistics.mean(ms_any) / 1e3) / 1e6, "unit": "Mrays/s"},
+            "render_1024x1024_16spp": {"ms_mean": 1e3 * statistics.mean(rt), "ms_min": 1e3 * min(rt),
+                                       "camera_rays": 1024 * 1024 * 16},
+            "bvh_host_build_s": build_s,
+        }
+        print(json.dumps(out))
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,233 @@
+/*
+ * pbrt_gpu.h - C ABI of the GB300 (sm_103a) implementation of pbrt_rust's
+ * data-parallel hot path: BVH traversal with triangle/sphere tests
+ * (closest hit and any hit), camera-ray generation from the stratified
+ * sampler, and the direct-lighting Li with shadow rays.
+ *
+ * Every entry point is plain C: pointers, sizes and an int status
+ * (0 == PBRT_OK).  No exception and no C++ or torch type crosses it.
+ * Handles are opaque.  A handle may be used from several host threads as
+ * long as every thread passes its own CUDA stream.
+ *
+ * Citations are to the reference crate (Mokosha/pbrt_rust), path:line.
+ */
+#ifndef PBRT_GPU_H
+#define PBRT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBRT_GPU_ABI_VERSION 1
+
+/* Status codes.  The reference signals failures with panic!/assert!
+ * (e.g. src/primitive/aggregates/bvh.rs:237-238); here they come back as
+ * codes and pbrtgpu_last_error() gives the detail. */
+typedef enum PbrtStatus {
+    PBRT_OK = 0,
+    PBRT_ERR_INVALID_ARGUMENT = 1,
+    PBRT_ERR_CUDA = 2,
+    PBRT_ERR_OUT_OF_MEMORY = 3,
+    PBRT_ERR_UNSUPPORTED = 4,
+    PBRT_ERR_BUILD = 5,          /* a BVH build invariant failed (bvh.rs:237-238) */
+    PBRT_ERR_STACK_OVERFLOW = 6, /* traversal stack too small for the tree depth */
+    PBRT_ERR_BUDGET = 7,         /* admission refused: device-memory budget */
+    PBRT_ERR_TIMEOUT = 8,        /* a bounded device-side wait ran out */
+    PBRT_ERR_NAN = 9,            /* a radiance sample was NaN (sampler_renderer.rs:105) */
+    PBRT_ERR_NO_DEVICE = 10,
+    PBRT_ERR_CANCELLED = 11
+} PbrtStatus;
+
+/* Ray: 32 bytes.  Mirrors src/ray.rs:8-15 (o, d, mint, maxt); time and
+ * depth are not needed by traversal. */
+typedef struct PbrtRay {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} PbrtRay;
+
+/* Closest hit: 16 bytes.  prim = index of the primitive in the fully
+ * refined input list (every mesh expands to its triangles in index order,
+ * src/shape/mesh.rs:325-335 + src/primitive/mod.rs:47-63), -1 on a miss.
+ * For triangles b1/b2 are the barycentrics of src/shape/mesh.rs:41-72;
+ * for spheres both are 0. */
+typedef struct PbrtHit {
+    int32_t prim;
+    float t;
+    float b1;
+    float b2;
+} PbrtHit;
+
+/* The reference Transform {m, m_inv} (src/transform/transform.rs:14-19),
+ * row-major 4x4 matrices. */
+typedef struct PbrtTransform {
+    float m[16];
+    float m_inv[16];
+} PbrtTransform;
+
+enum { PBRT_SHAPE_TRIANGLE_MESH = 0, PBRT_SHAPE_SPHERE = 1 };
+enum { PBRT_SPLIT_SAH = 0, PBRT_SPLIT_MIDDLE = 1, PBRT_SPLIT_EQUAL = 2 };
+
+/* One input primitive.  Mirrors Shape::triangle_mesh and Shape::sphere
+ * (src/shape/mod.rs:170-190) wrapped by Primitive::geometric
+ * (src/primitive/mod.rs:87-99).  world_to_object is taken as the
+ * inverse of object_to_world, i.e. Transform{m_inv, m}. */
+typedef struct PbrtShapeDesc {
+    int32_t kind;                 /* PBRT_SHAPE_* */
+    int32_t reverse_orientation;
+    PbrtTransform object_to_world;
+    /* triangle mesh (object space; transformed to world at creation,
+     * src/shape/mesh.rs:299-314) */
+    const float* points;          /* 3 * n_points floats */
+    uint32_t n_points;
+    const uint32_t* indices;      /* n_indices, a multiple of 3 */
+    uint32_t n_indices;
+    /* sphere (src/shape/sphere.rs:28-44) */
+    float radius, z0, z1, phi_max_deg;
+    /* render-only */
+    int32_t material;             /* index into PbrtSceneDesc.materials */
+    int32_t area_light;           /* index into PbrtSceneDesc.lights or -1 */
+} PbrtShapeDesc;
+
+/* Matte material (src/material/matte.rs:30-51) with constant textures. */
+typedef struct PbrtMaterialDesc {
+    float kd[3];
+    float sigma;                  /* only 0 (Lambertian) is supported */
+} PbrtMaterialDesc;
+
+enum { PBRT_LIGHT_POINT = 0, PBRT_LIGHT_DIFFUSE_AREA = 1 };
+
+/* Point light (src/light/point.rs:16-35) or a diffuse area light over the
+ * triangles of one mesh shape (src/area_light.rs is a stub in the
+ * reference; this follows pbrt-v2's DiffuseAreaLight). */
+typedef struct PbrtLightDesc {
+    int32_t kind;                 /* PBRT_LIGHT_* */
+    PbrtTransform light_to_world; /* point: position = light_to_world(0,0,0) */
+    float spectrum[3];            /* point: intensity; area: emitted radiance */
+    int32_t shape;                /* area: index of the emitting mesh shape */
+} PbrtLightDesc;
+
+typedef struct PbrtSceneDesc {
+    const PbrtShapeDesc* shapes;
+    uint32_t n_shapes;
+    const PbrtMaterialDesc* materials;
+    uint32_t n_materials;
+    const PbrtLightDesc* lights;
+    uint32_t n_lights;
+    uint32_t max_prims_in_node;   /* BVHAccelerator::new mp (bvh.rs:335) */
+    int32_t split_method;         /* PBRT_SPLIT_* */
+} PbrtSceneDesc;
+
+/* Perspective camera (src/camera/mod.rs:105-135) with an image film
+ * (src/camera/film.rs:77-122) and a box filter (src/filter.rs:45-50). */
+typedef struct PbrtCameraDesc {
+    PbrtTransform camera_to_world; /* static: AnimatedTransform of equal ends */
+    float fov_deg;
+    float screen_window[4];
+    float lens_radius, focal_distance;
+    float shutter_open, shutter_close;
+    uint32_t x_res, y_res;
+    float crop_window[4];
+    float filter_x_width, filter_y_width;
+} PbrtCameraDesc;
+
+/* Stratified sampler (src/sampler/stratified.rs:23-37) and the task count
+ * of SamplerRenderer (src/sampler_renderer.rs:39-44), given explicitly so
+ * the random streams do not depend on the host's core count. */
+typedef struct PbrtSamplerDesc {
+    int32_t x_start, x_end, y_start, y_end;
+    uint32_t x_samples, y_samples;
+    int32_t jitter;
+    float shutter_open, shutter_close;
+    uint32_t num_tasks;
+} PbrtSamplerDesc;
+
+/* One node of the reference's linearised BVH (PackedBVHNode,
+ * src/primitive/aggregates/bvh.rs:260-326), exported for inspection. */
+typedef struct PbrtPackedNode {
+    float lo[3];
+    float hi[3];
+    int32_t is_leaf;
+    uint32_t offset;     /* leaf: prim_offset; inner: second_child_offset */
+    uint32_t count;      /* leaf: num_prims; inner: split axis */
+} PbrtPackedNode;
+
+typedef struct PbrtBVH PbrtBVH;
+typedef struct PbrtScene PbrtScene;
+
+/* ---- library ---------------------------------------------------------- */
+
+int pbrtgpu_abi_version(void);
+const char* pbrtgpu_status_str(int status);
+/* Detail of the last failing call on this host thread ("" if none). */
+const char* pbrtgpu_last_error(void);
+
+/* ---- aggregate: the GpuBVHAccel drop-in ------------------------------- */
+
+/* Replaces BVHAccelerator::new(p, mp, sm)
+ * (src/primitive/aggregates/bvh.rs:334-363) and Aggregate::bvh
+ * (src/primitive/aggregates/mod.rs:27-29).  The primitives are fully
+ * refined, the SAH/middle/equal tree is built on the host with the
+ * reference's arithmetic, flattened, and uploaded to the current device.
+ * An unknown split_method falls back to "sah" with a warning, as
+ * bvh.rs:341-349 does. */
+int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
+                       uint32_t max_prims_in_node, const char* split_method,
+                       PbrtBVH** out);
+void pbrtgpu_bvh_destroy(PbrtBVH* bvh);
+
+/* Replaces HasBounds::world_bound for BVHAccelerator (bvh.rs:365-373). */
+int pbrtgpu_bvh_world_bound(const PbrtBVH* bvh, float lo[3], float hi[3]);
+int pbrtgpu_bvh_num_primitives(const PbrtBVH* bvh, uint32_t* n);
+int pbrtgpu_bvh_num_nodes(const PbrtBVH* bvh, uint32_t* n);
+int pbrtgpu_bvh_depth(const PbrtBVH* bvh, uint32_t* depth);
+/* The reference-order linearised nodes (bvh.rs:319-325). */
+int pbrtgpu_bvh_get_nodes(const PbrtBVH* bvh, PbrtPackedNode* out,
+                          uint32_t capacity);
+/* ordered_prims of bvh.rs:356: out[i] = input index of the i-th primitive. */
+int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* bvh, uint32_t* out,
+                                    uint32_t capacity);
+
+/* Replaces Intersectable::intersect for the BVH (bvh.rs:375-422) over a
+ * batch of rays: closest hit per ray.  rays/hits may be device pointers
+ * or host pointers (pinned or pageable); host buffers are staged through
+ * the device with the copies on `stream`.  The call returns after the
+ * work is queued for device buffers and after completion for host
+ * buffers.  `stream` is a cudaStream_t (NULL = legacy default stream). */
+int pbrtgpu_intersect(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
+                      PbrtHit* hits, void* stream);
+
+/* Replaces Intersectable::intersect_p (src/intersection.rs:61-66) for the
+ * BVH: occluded[i] = 1 if any primitive is hit within [tmin, tmax]. */
+int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
+                        uint8_t* occluded, void* stream);
+
+/* ---- renderer: the GpuSamplerRenderer drop-in ------------------------- */
+
+/* Builds the aggregate plus the device copies of materials and lights
+ * (Scene::new_with, src/scene.rs:31-39). */
+int pbrtgpu_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
+void pbrtgpu_scene_destroy(PbrtScene* scene);
+/* The scene's aggregate, usable with pbrtgpu_intersect*. */
+int pbrtgpu_scene_bvh(const PbrtScene* scene, const PbrtBVH** out);
+
+/* Replaces Renderer::render for SamplerRenderer
+ * (src/sampler_renderer.rs:147-182, run_task :61-144, li :184-206) as a
+ * wavefront: generate -> extend -> shade -> shadow -> accumulate.
+ * rgb_out receives the film's pixel extent (film.rs:301-309) as linear
+ * float RGB, 3 floats per pixel, row-major; host or device pointer. */
+int pbrtgpu_render(const PbrtScene* scene, const PbrtCameraDesc* camera,
+                   const PbrtSamplerDesc* sampler, float* rgb_out,
+                   void* stream);
+
+/* Pixel extent (x0, x1, y0, y1) of the film a camera describes
+ * (Film::get_pixel_extent, src/camera/film.rs:301-309). */
+int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* camera, int32_t ext[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBRT_GPU_H */

@@ -1,0 +1,275 @@
+// capi.cu - the C ABI declared in include/pbrt_gpu.h.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/pbrt_gpu.h"
+#include "capi_internal.h"
+#include "host_scene.h"
+#include "kernels.h"
+
+using namespace pbrt;
+
+namespace pbrt {
+
+static thread_local std::string g_last_error;
+
+int set_error(int status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return PBRT_OK;
+    int st = (e == cudaErrorMemoryAllocation) ? PBRT_ERR_OUT_OF_MEMORY
+             : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? PBRT_ERR_NO_DEVICE
+                                                                              : PBRT_ERR_CUDA;
+    return set_error(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int DeviceBuf::reserve(size_t bytes) {
+    if (cap >= bytes) return PBRT_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    int st = cuda_status(cudaMalloc(&p, want), "cudaMalloc");
+    if (st) return st;
+    cap = want;
+    return PBRT_OK;
+}
+void DeviceBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+
+bool is_device_pointer(const void* ptr) {
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+DeviceGuard::DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        prev = -1;
+    }
+    if (prev != dev) cudaSetDevice(dev);
+}
+DeviceGuard::~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+}
+
+template <class T>
+static int upload(T** dst, const std::vector<T>& src) {
+    *dst = nullptr;
+    if (src.empty()) return PBRT_OK;
+    int st = cuda_status(cudaMalloc((void**)dst, src.size() * sizeof(T)), "cudaMalloc");
+    if (st) return st;
+    return cuda_status(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+}
+
+int bvh_upload(PbrtBVH* b) {
+    std::lock_guard<std::mutex> lk(b->upload_mu);
+    if (b->uploaded) return PBRT_OK;
+    int st;
+    if ((st = cuda_status(cudaGetDevice(&b->device), "cudaGetDevice"))) return st;
+    if ((st = upload(&b->d_pairs, b->host.pairs))) return st;
+    if ((st = upload(&b->d_prims, b->host.recs))) return st;
+    if ((st = upload(&b->d_spheres, b->host.spheres))) return st;
+    if ((st = cuda_status(cudaMalloc(&b->d_status, sizeof(int)), "cudaMalloc"))) return st;
+    if ((st = cuda_status(cudaMemset(b->d_status, 0, sizeof(int)), "cudaMemset"))) return st;
+    b->dev.pairs = b->d_pairs;
+    b->dev.prims = b->d_prims;
+    b->dev.spheres = b->d_spheres;
+    b->dev.root = b->host.root;
+    b->dev.has_spheres = b->host.has_spheres ? 1u : 0u;
+    b->dev.n_prims = (uint32_t)b->host.recs.size();
+    b->dev.empty = b->host.nodes.empty() ? 1u : 0u;
+    b->uploaded = true;
+    return PBRT_OK;
+}
+
+// Runs closest/any hit for host or device buffers.
+static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHit* hits, uint8_t* occ,
+                      void* stream_v) {
+    PbrtBVH* b = const_cast<PbrtBVH*>(cb);
+    if (!b) return set_error(PBRT_ERR_INVALID_ARGUMENT, "bvh is NULL");
+    if (n == 0) return PBRT_OK;
+    if (!rays || (!hits && !occ)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "rays/output is NULL");
+    int st;
+    if (!b->uploaded && (st = bvh_upload(b))) return st;
+    DeviceGuard g(b->device);
+    cudaStream_t s = (cudaStream_t)stream_v;
+    void* out = hits ? (void*)hits : (void*)occ;
+    size_t out_bytes = hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n;
+    bool dr = is_device_pointer(rays), dout = is_device_pointer(out);
+    if (dr && dout)
+        return cuda_status(launch_trace(b->dev, b->host.depth, rays, n, hits, occ, b->d_status, s), "trace launch");
+    std::lock_guard<std::mutex> lk(b->stage_mu);
+    const PbrtRay* d_rays = rays;
+    if (!dr) {
+        if ((st = b->stage_in.reserve((size_t)n * sizeof(PbrtRay)))) return st;
+        if ((st = cuda_status(cudaMemcpyAsync(b->stage_in.p, rays, (size_t)n * sizeof(PbrtRay),
+                                              cudaMemcpyHostToDevice, s),
+                              "cudaMemcpyAsync H2D")))
+            return st;
+        d_rays = (const PbrtRay*)b->stage_in.p;
+    }
+    void* d_out = out;
+    if (!dout) {
+        if ((st = b->stage_out.reserve(out_bytes))) return st;
+        d_out = b->stage_out.p;
+    }
+    if ((st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, hits ? (PbrtHit*)d_out : nullptr,
+                                       hits ? nullptr : (uint8_t*)d_out, b->d_status, s),
+                          "trace launch")))
+        return st;
+    if (!dout &&
+        (st = cuda_status(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H")))
+        return st;
+    if ((st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"))) return st;
+    int dev_status = 0;
+    if ((st = cuda_status(cudaMemcpy(&dev_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status")))
+        return st;
+    if (dev_status) {
+        cudaMemset(b->d_status, 0, sizeof(int));
+        return set_error(dev_status, "device-side traversal failure");
+    }
+    return PBRT_OK;
+}
+
+}  // namespace pbrt
+
+PbrtBVH::~PbrtBVH() {
+    if (d_pairs) cudaFree(d_pairs);
+    if (d_prims) cudaFree(d_prims);
+    if (d_spheres) cudaFree(d_spheres);
+    if (d_status) cudaFree(d_status);
+    stage_in.release();
+    stage_out.release();
+}
+
+extern "C" {
+
+int pbrtgpu_abi_version(void) { return PBRT_GPU_ABI_VERSION; }
+
+const char* pbrtgpu_status_str(int s) {
+    switch (s) {
+        case PBRT_OK: return "ok";
+        case PBRT_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PBRT_ERR_CUDA: return "CUDA error";
+        case PBRT_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case PBRT_ERR_UNSUPPORTED: return "unsupported";
+        case PBRT_ERR_BUILD: return "BVH build failed";
+        case PBRT_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+        case PBRT_ERR_BUDGET: return "device-memory budget exceeded";
+        case PBRT_ERR_TIMEOUT: return "device wait timed out";
+        case PBRT_ERR_NAN: return "NaN radiance";
+        case PBRT_ERR_NO_DEVICE: return "no CUDA device";
+        case PBRT_ERR_CANCELLED: return "cancelled";
+        default: return "unknown status";
+    }
+}
+
+const char* pbrtgpu_last_error(void) { return pbrt::g_last_error.c_str(); }
+
+int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
+                       PbrtBVH** out) {
+    if (!out || (!shapes && n_shapes)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    PbrtBVH* b = new PbrtBVH();
+    std::string err;
+    int st = build_host_bvh(shapes, n_shapes, max_prims, split_method, &b->host, &err);
+    if (st) {
+        delete b;
+        return set_error(st, err);
+    }
+    if (trace_stack_for_depth(b->host.depth) == 0) {
+        std::string msg = "BVH depth " + std::to_string(b->host.depth) + " exceeds the deepest traversal stack (256)";
+        delete b;
+        return set_error(PBRT_ERR_STACK_OVERFLOW, msg);
+    }
+    *out = b;
+    return PBRT_OK;
+}
+
+void pbrtgpu_bvh_destroy(PbrtBVH* b) {
+    if (!b) return;
+    DeviceGuard g(b->device);
+    delete b;
+}
+
+int pbrtgpu_bvh_world_bound(const PbrtBVH* b, float lo[3], float hi[3]) {
+    if (!b || !lo || !hi) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    Box bx = b->host.nodes.empty() ? box_empty() : b->host.nodes[0].box;  // bvh.rs:365-373
+    lo[0] = bx.lo.x;
+    lo[1] = bx.lo.y;
+    lo[2] = bx.lo.z;
+    hi[0] = bx.hi.x;
+    hi[1] = bx.hi.y;
+    hi[2] = bx.hi.z;
+    return PBRT_OK;
+}
+
+int pbrtgpu_bvh_num_primitives(const PbrtBVH* b, uint32_t* n) {
+    if (!b || !n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *n = (uint32_t)b->host.prims.size();
+    return PBRT_OK;
+}
+int pbrtgpu_bvh_num_nodes(const PbrtBVH* b, uint32_t* n) {
+    if (!b || !n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *n = (uint32_t)b->host.nodes.size();
+    return PBRT_OK;
+}
+int pbrtgpu_bvh_depth(const PbrtBVH* b, uint32_t* d) {
+    if (!b || !d) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    *d = b->host.depth;
+    return PBRT_OK;
+}
+int pbrtgpu_bvh_get_nodes(const PbrtBVH* b, PbrtPackedNode* out, uint32_t cap) {
+    if (!b || (!out && !b->host.nodes.empty())) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cap < b->host.nodes.size()) return set_error(PBRT_ERR_INVALID_ARGUMENT, "capacity too small");
+    for (size_t i = 0; i < b->host.nodes.size(); ++i) {
+        const FlatNode& n = b->host.nodes[i];
+        PbrtPackedNode& o = out[i];
+        o.lo[0] = n.box.lo.x;
+        o.lo[1] = n.box.lo.y;
+        o.lo[2] = n.box.lo.z;
+        o.hi[0] = n.box.hi.x;
+        o.hi[1] = n.box.hi.y;
+        o.hi[2] = n.box.hi.z;
+        o.is_leaf = n.leaf ? 1 : 0;
+        o.offset = n.offset;
+        o.count = n.count;
+    }
+    return PBRT_OK;
+}
+int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t cap) {
+    if (!b || (!out && !b->host.ordered.empty())) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (cap < b->host.ordered.size()) return set_error(PBRT_ERR_INVALID_ARGUMENT, "capacity too small");
+    if (!b->host.ordered.empty()) std::memcpy(out, b->host.ordered.data(), b->host.ordered.size() * sizeof(uint32_t));
+    return PBRT_OK;
+}
+
+int pbrtgpu_intersect(const PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit* hits, void* stream) {
+    if (!hits && n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "hits is NULL");
+    return trace_call(b, rays, n, hits, nullptr, stream);
+}
+
+int pbrtgpu_intersect_p(const PbrtBVH* b, const PbrtRay* rays, uint32_t n, uint8_t* occluded, void* stream) {
+    if (!occluded && n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "occluded is NULL");
+    return trace_call(b, rays, n, nullptr, occluded, stream);
+}
+
+}  // extern "C"

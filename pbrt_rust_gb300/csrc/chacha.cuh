@@ -1,0 +1,103 @@
+// chacha.cuh - the reference RNG stream on the device.
+//
+// src/rng.rs wraps rand 0.8.5's StdRng, which is ChaCha with 12 rounds
+// (rand_chacha 0.3.1): 16-word state of the four constants, the 8-word key,
+// a 64-bit block counter (words 12-13) and a zero 64-bit stream id (words
+// 14-15); output words are the keystream words in order.  Because the
+// keystream is a function of the block counter, a thread seeks directly to
+// the first word of its pixel instead of replaying the task's stream.
+// The key is expanded on the host from the task index (rand_core 0.6.4
+// seed_from_u64, see host_scene.cpp).
+#pragma once
+#include <stdint.h>
+
+namespace pbrt {
+
+__device__ __forceinline__ uint32_t rotl32(uint32_t v, int c) { return __funnelshift_l(v, v, c); }
+
+#define PBRT_QR(a, b, c, d) \
+    a += b;                 \
+    d ^= a;                 \
+    d = rotl32(d, 16);      \
+    c += d;                 \
+    b ^= c;                 \
+    b = rotl32(b, 12);      \
+    a += b;                 \
+    d ^= a;                 \
+    d = rotl32(d, 8);       \
+    c += d;                 \
+    b ^= c;                 \
+    b = rotl32(b, 7);
+
+__device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr, uint32_t out[16]) {
+    uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
+    uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
+    uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
+    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = 0u, x15 = 0u;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        PBRT_QR(x0, x4, x8, x12);
+        PBRT_QR(x1, x5, x9, x13);
+        PBRT_QR(x2, x6, x10, x14);
+        PBRT_QR(x3, x7, x11, x15);
+        PBRT_QR(x0, x5, x10, x15);
+        PBRT_QR(x1, x6, x11, x12);
+        PBRT_QR(x2, x7, x8, x13);
+        PBRT_QR(x3, x4, x9, x14);
+    }
+    out[0] = x0 + 0x61707865u;
+    out[1] = x1 + 0x3320646eu;
+    out[2] = x2 + 0x79622d32u;
+    out[3] = x3 + 0x6b206574u;
+    out[4] = x4 + key[0];
+    out[5] = x5 + key[1];
+    out[6] = x6 + key[2];
+    out[7] = x7 + key[3];
+    out[8] = x8 + key[4];
+    out[9] = x9 + key[5];
+    out[10] = x10 + key[6];
+    out[11] = x11 + key[7];
+    out[12] = x12 + (uint32_t)ctr;
+    out[13] = x13 + (uint32_t)(ctr >> 32);
+    out[14] = x14;
+    out[15] = x15;
+}
+#undef PBRT_QR
+
+// A seekable reader of one task's word stream.
+struct WordStream {
+    uint32_t key[8];
+    uint64_t block;
+    uint32_t buf[16];
+    int idx;
+
+    __device__ void seek(const uint32_t* k, uint64_t word) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) key[i] = k[i];
+        block = word >> 4;
+        idx = (int)(word & 15);
+        chacha12_block(key, block, buf);
+    }
+    __device__ __forceinline__ uint32_t next_u32() {
+        if (idx == 16) {
+            ++block;
+            chacha12_block(key, block, buf);
+            idx = 0;
+        }
+        return buf[idx++];
+    }
+    __device__ __forceinline__ uint64_t next_u64() {  // low word first
+        uint64_t lo = next_u32();
+        uint64_t hi = next_u32();
+        return lo | (hi << 32);
+    }
+    // rng.rs:15-17 - gen::<f32>(): (u32 >> 8) * 2^-24
+    __device__ __forceinline__ float random_float() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+    // rng.rs:19-21
+    __device__ __forceinline__ uint64_t random_uint() {
+        uint64_t v = next_u64();
+        return v == 0xFFFFFFFFFFFFFFFFull ? 0ull : v;  // v % usize::MAX
+    }
+};
+
+}  // namespace pbrt

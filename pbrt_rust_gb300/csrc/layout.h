@@ -1,0 +1,64 @@
+// layout.h - device data layout of a flattened BVH scene (host + device).
+//
+// The reference keeps a depth-first array of PackedBVHNode
+// (src/primitive/aggregates/bvh.rs:260-326): first child at n+1, second
+// child at second_child_offset.  On the device the same tree is stored as
+// sibling PAIRS: every inner node owns one 64-byte pair holding its two
+// children's 32-byte records (child1 first), so one visit fetches both
+// child boxes.  Pairs are numbered in the depth-first pre-order of their
+// parents.  The root's own record travels in the kernel arguments.
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define PBRT_HD __host__ __device__ __forceinline__
+#else
+#define PBRT_HD inline
+#endif
+
+namespace pbrt {
+
+// 32-byte child record: box + two words.
+//   inner child: a = index of its own children's pair, b = its split axis
+//   leaf child:  a = first ordered primitive,        b = kLeafBit | count
+struct alignas(16) ChildRec {
+    float lo_x, lo_y, lo_z;
+    uint32_t a;
+    float hi_x, hi_y, hi_z;
+    uint32_t b;
+};
+static_assert(sizeof(ChildRec) == 32, "child record is 32 bytes");
+
+struct alignas(64) NodePair {
+    ChildRec c[2];
+};
+static_assert(sizeof(NodePair) == 64, "node pair is 64 bytes");
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kCountMask = 0x7fffffffu;
+
+// 48-byte primitive record in BVH (ordered) order.  Triangle: p1 and the
+// edges e1 = p2 - p1, e2 = p3 - p1, computed on the host with the same f32
+// subtraction the reference does per test (src/shape/mesh.rs:45-46).
+//   r0 = (p1.xyz, id)  id = refined input index | kSphereBit if a sphere
+//   r1 = (e1.xyz, sphere index bits for spheres)
+//   r2 = (e2.xyz, 0)
+struct alignas(16) PrimRec {
+    float r0[4];
+    float r1[4];
+    float r2[4];
+};
+static_assert(sizeof(PrimRec) == 48, "primitive record is 48 bytes");
+constexpr uint32_t kSphereBit = 0x80000000u;
+
+// Sphere (src/shape/sphere.rs:16-25) with its world-to-object matrix rows.
+struct alignas(16) SphereRec {
+    float w2o[16];      // row-major world_to_object.m
+    float o2w[16];      // row-major object_to_world.m
+    float radius, z_min, z_max, phi_max;
+    float theta_min, theta_max;
+    uint32_t full;      // no z or phi clipping can apply
+    uint32_t flip;      // reverse_orientation ^ transform_swaps_handedness
+};
+
+}  // namespace pbrt

@@ -1,0 +1,309 @@
+// trace.cuh - device BVH traversal (closest hit and any hit).
+//
+// Semantics follow BVHAccelerator::intersect
+// (src/primitive/aggregates/bvh.rs:375-422) exactly:
+//  * the slab test of src/bbox.rs:185-209 with inv_dir = 1/d per axis,
+//    fmaxf/fminf (Rust f32::max/min) and the reference operation order;
+//  * the Moller-Trumbore test of src/shape/mesh.rs:41-72 with inclusive
+//    [mint, maxt] and maxt shrunk to every accepted hit
+//    (src/primitive/geometric.rs:64), so a later primitive at equal t
+//    replaces an earlier one;
+//  * the sphere test of src/shape/sphere.rs:46-107 in object space;
+//  * the reference visiting order: the child that BVHAccelerator pops
+//    first (child1 unless dir_is_neg[axis]) is traversed first.
+// Instead of testing a node's box when it is popped, both child boxes are
+// tested at the parent (one 64-byte pair fetch) and the deferred child is
+// pushed with its entry distance t0.  A box test passes iff
+// t0 <= min(far planes, maxt); t0 does not depend on maxt and the far part
+// was checked at push time, so re-checking t0 <= maxt at pop gives the
+// reference's decision.  Hit indices, t and barycentrics are therefore the
+// reference's bit for bit (the library is built with --fmad=false and
+// IEEE division/sqrt).
+#pragma once
+#include <stdint.h>
+
+#include "layout.h"
+
+namespace pbrt {
+
+struct DevBVH {
+    const NodePair* pairs;
+    const PrimRec* prims;
+    const SphereRec* spheres;
+    ChildRec root;
+    uint32_t has_spheres;
+    uint32_t n_prims;
+    uint32_t empty;
+};
+
+struct DRay {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+    float ix, iy, iz;  // 1/d
+    uint32_t neg;      // bit i: inv_dir[i] < 0 (bvh.rs:383)
+};
+
+__device__ __forceinline__ DRay make_dray(float4 a, float4 b) {
+    DRay r;
+    r.ox = a.x;
+    r.oy = a.y;
+    r.oz = a.z;
+    r.tmin = a.w;
+    r.dx = b.x;
+    r.dy = b.y;
+    r.dz = b.z;
+    r.tmax = b.w;
+    r.ix = 1.0f / r.dx;
+    r.iy = 1.0f / r.dy;
+    r.iz = 1.0f / r.dz;
+    r.neg = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
+    return r;
+}
+
+// src/bbox.rs:185-209 for one box; returns t0 in *t_enter on a pass.
+__device__ __forceinline__ bool slab(float lox, float loy, float loz, float hix, float hiy, float hiz, const DRay& r,
+                                     float maxt, float* t_enter) {
+    float t0 = r.tmin, t1 = maxt;
+    float ta = (lox - r.ox) * r.ix, tb = (hix - r.ox) * r.ix;
+    float tn = ta > tb ? tb : ta, tf = ta > tb ? ta : tb;
+    t0 = fmaxf(tn, t0);
+    t1 = fminf(tf, t1);
+    ta = (loy - r.oy) * r.iy;
+    tb = (hiy - r.oy) * r.iy;
+    tn = ta > tb ? tb : ta;
+    tf = ta > tb ? ta : tb;
+    t0 = fmaxf(tn, t0);
+    t1 = fminf(tf, t1);
+    ta = (loz - r.oz) * r.iz;
+    tb = (hiz - r.oz) * r.iz;
+    tn = ta > tb ? tb : ta;
+    tf = ta > tb ? ta : tb;
+    t0 = fmaxf(tn, t0);
+    t1 = fminf(tf, t1);
+    *t_enter = t0;
+    return !(t0 > t1);
+}
+
+// src/shape/mesh.rs:41-72 with e1, e2 precomputed (same f32 subtraction).
+__device__ __forceinline__ bool tri_test(float4 r0, float4 r1, float4 r2, const DRay& r, float maxt, float* t_out,
+                                         float* b1_out, float* b2_out) {
+    float e1x = r1.x, e1y = r1.y, e1z = r1.z;
+    float e2x = r2.x, e2y = r2.y, e2z = r2.z;
+    float s1x = (r.dy * e2z) - (r.dz * e2y);
+    float s1y = (r.dz * e2x) - (r.dx * e2z);
+    float s1z = (r.dx * e2y) - (r.dy * e2x);
+    float divisor = s1x * e1x + s1y * e1y + s1z * e1z;
+    if (divisor == 0.0f) return false;
+    float inv = 1.0f / divisor;
+    float sx = r.ox - r0.x, sy = r.oy - r0.y, sz = r.oz - r0.z;
+    float b1 = (s1x * sx + s1y * sy + s1z * sz) * inv;
+    if (b1 < 0.0f || b1 > 1.0f) return false;
+    float s2x = (sy * e1z) - (sz * e1y);
+    float s2y = (sz * e1x) - (sx * e1z);
+    float s2z = (sx * e1y) - (sy * e1x);
+    float b2 = (r.dx * s2x + r.dy * s2y + r.dz * s2z) * inv;
+    if (b2 < 0.0f || (b1 + b2) > 1.0f) return false;
+    float t = (e2x * s2x + e2y * s2y + e2z * s2z) * inv;
+    if (t < r.tmin || t > maxt) return false;
+    *t_out = t;
+    *b1_out = b1;
+    *b2_out = b2;
+    return true;
+}
+
+// src/transform/transform.rs:195-218 (point with the w != 1 divide; vector)
+__device__ __forceinline__ void xf_point(const float* m, float x, float y, float z, float* o) {
+    float xt = m[0] * x + m[1] * y + m[2] * z + m[3];
+    float yt = m[4] * x + m[5] * y + m[6] * z + m[7];
+    float zt = m[8] * x + m[9] * y + m[10] * z + m[11];
+    float w = m[12] * x + m[13] * y + m[14] * z + m[15];
+    if (w != 1.0f) {
+        xt = xt / w;
+        yt = yt / w;
+        zt = zt / w;
+    }
+    o[0] = xt;
+    o[1] = yt;
+    o[2] = zt;
+}
+__device__ __forceinline__ void xf_vector(const float* m, float x, float y, float z, float* o) {
+    o[0] = m[0] * x + m[1] * y + m[2] * z;
+    o[1] = m[4] * x + m[5] * y + m[6] * z;
+    o[2] = m[8] * x + m[9] * y + m[10] * z;
+}
+
+// src/utils/mod.rs:56-92
+__device__ __forceinline__ bool quadratic(float a, float b, float c, float* t0, float* t1) {
+    float descrim = b * b - 4.0f * a * c;
+    if (descrim < 0.0f) return false;
+    if (fabsf(descrim) < 1e-6f) {
+        if (a == 0.0f) return false;
+        float t = -b / (2.0f * a);
+        *t0 = t;
+        *t1 = t;
+        return true;
+    }
+    float root = sqrtf(descrim);
+    float q = b < 0.0f ? -0.5f * (b - root) : -0.5f * (b + root);
+    if (a == 0.0f) return false;
+    float r0 = q / a, r1 = c / q;
+    if (r0 < r1) {
+        *t0 = r0;
+        *t1 = r1;
+    } else {
+        *t0 = r1;
+        *t1 = r0;
+    }
+    return true;
+}
+
+// src/shape/sphere.rs:46-107 on the object-space ray (o, d).  For full
+// spheres the clip test cannot reject (see SphereRec::full) and is
+// skipped; partial spheres evaluate it with CUDA's atan2f.
+__device__ __forceinline__ bool sphere_obj_test(const SphereRec& s, const float* o, const float* d, float mint,
+                                                float maxt, float* t_out) {
+    float a = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    float b = 2.0f * (d[0] * o[0] + d[1] * o[1] + d[2] * o[2]);
+    float c = (o[0] * o[0] + o[1] * o[1] + o[2] * o[2]) - s.radius * s.radius;
+    float t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0 > maxt || t1 < mint) return false;
+    float th = t0;
+    if (t0 < mint) {
+        th = t1;
+        if (th > maxt) return false;
+    }
+    if (!s.full) {
+        auto invalid = [&](float t) {
+            float hx = o[0] + d[0] * t, hy = o[1] + d[1] * t, hz = o[2] + d[2] * t;
+            if (hx == 0.0f && hy == 0.0f) hx = 1e-5f * s.radius;
+            float phi = atan2f(hy, hx);
+            if (phi < 0.0f) phi += 2.0f * 3.14159265358979323846f;
+            return (hz > -s.radius && hz < s.z_min) || (hz < s.radius && hz > s.z_max) || (phi > s.phi_max);
+        };
+        if (invalid(th)) {
+            if (th == t1) return false;
+            if (t1 > maxt) return false;
+            th = t1;
+            if (invalid(th)) return false;
+        }
+    }
+    *t_out = th;
+    return true;
+}
+
+__device__ __forceinline__ bool sphere_test(const SphereRec* spheres, uint32_t si, const DRay& r, float maxt,
+                                            float* t_out) {
+    const SphereRec& s = spheres[si];
+    float o[3], d[3];
+    xf_point(s.w2o, r.ox, r.oy, r.oz, o);
+    xf_vector(s.w2o, r.dx, r.dy, r.dz, d);
+    return sphere_obj_test(s, o, d, r.tmin, maxt, t_out);
+}
+
+__device__ __forceinline__ float4 ldg4(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+struct TraceResult {
+    int32_t prim;
+    float t, b1, b2;
+};
+
+// Closest hit (ANY = false) or any hit (ANY = true).  `status` gets
+// PBRT_ERR_STACK_OVERFLOW (6) if the stack would overflow (the host checks
+// the tree depth first, so this only guards).
+template <int STACK, bool ANY>
+__device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status) {
+    float maxt = r.tmax;
+    bool found = false;
+    res->prim = -1;
+    res->t = 0.0f;
+    res->b1 = 0.0f;
+    res->b2 = 0.0f;
+    if (bvh.empty) return false;
+    float tr;
+    const ChildRec& R = bvh.root;
+    if (!slab(R.lo_x, R.lo_y, R.lo_z, R.hi_x, R.hi_y, R.hi_z, r, maxt, &tr)) return false;
+    uint32_t a = R.a, b = R.b;
+    uint32_t st_a[STACK];
+    uint32_t st_b[STACK];
+    float st_t[STACK];
+    int sp = 0;
+    for (;;) {
+        if (b & kLeafBit) {
+            uint32_t cnt = b & kCountMask;
+            for (uint32_t i = 0; i < cnt; ++i) {
+                const PrimRec* pr = bvh.prims + a + i;
+                float4 r0 = ldg4(pr->r0);
+                uint32_t id = __float_as_uint(r0.w);
+                float t, b1 = 0.0f, b2 = 0.0f;
+                bool hit;
+                if (id & kSphereBit) {
+                    float4 r1 = ldg4(pr->r1);
+                    hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
+                } else {
+                    float4 r1 = ldg4(pr->r1), r2 = ldg4(pr->r2);
+                    hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
+                }
+                if (hit) {
+                    maxt = t;
+                    found = true;
+                    res->prim = (int32_t)(id & ~kSphereBit);
+                    res->t = t;
+                    res->b1 = b1;
+                    res->b2 = b2;
+                    if (ANY) return true;
+                }
+            }
+        } else {
+            const NodePair* np = bvh.pairs + a;
+            float4 c0a = ldg4(&np->c[0].lo_x), c0b = ldg4(&np->c[0].hi_x);
+            float4 c1a = ldg4(&np->c[1].lo_x), c1b = ldg4(&np->c[1].hi_x);
+            float t0, t1;
+            bool h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
+            bool h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+            // Near child: child1 unless dir_is_neg[axis] (bvh.rs:409-415).
+            bool swap = (r.neg >> b) & 1u;
+            uint32_t na = swap ? __float_as_uint(c1a.w) : __float_as_uint(c0a.w);
+            uint32_t nb = swap ? __float_as_uint(c1b.w) : __float_as_uint(c0b.w);
+            uint32_t fa = swap ? __float_as_uint(c0a.w) : __float_as_uint(c1a.w);
+            uint32_t fb = swap ? __float_as_uint(c0b.w) : __float_as_uint(c1b.w);
+            bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
+            float tf = swap ? t0 : t1;
+            if (hn) {
+                if (hf) {
+                    if (sp == STACK) {
+                        *status = 6;
+                        return found;
+                    }
+                    st_a[sp] = fa;
+                    st_b[sp] = fb;
+                    st_t[sp] = tf;
+                    ++sp;
+                }
+                a = na;
+                b = nb;
+                continue;
+            }
+            if (hf) {
+                a = fa;
+                b = fb;
+                continue;
+            }
+        }
+        // pop the next deferred child whose box still passes
+        bool next = false;
+        while (sp > 0) {
+            --sp;
+            if (!(st_t[sp] > maxt)) {
+                a = st_a[sp];
+                b = st_b[sp];
+                next = true;
+                break;
+            }
+        }
+        if (!next) break;
+    }
+    return found;
+}
+
+}  // namespace pbrt

@@ -1,0 +1,237 @@
+"""Seeded synthetic workloads (the reference ships no scenes or datasets).
+
+Random numbers come from PCG32 (O'Neill 2014, XSH-RR output, the
+pcg32_srandom_r seeding with a stream selector), vectorised with the
+closed-form LCG jump so that large scenes generate quickly; each config's
+seed is 0x9E3779B9 ^ config_index ^ (scene_index << 8).  Uniform floats
+are (u32 >> 8) * 2^-24.  Geometry is computed in float64 and stored as
+float32.
+
+  ray_soup      4096 random triangles + 2^20 rays toward the centre
+  c1_scene      512x512 render: ground quad, 64 matte spheres, point light,
+                quad area light, 2x2 jittered strata
+  heightfield   708x708-vertex terrain (999,698 triangles) + area light,
+                1024x1024 at 16 spp, and 2^22 incoherent rays
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+from .scene import (Camera, DiffuseAreaLight, Film, Filter, MatteMaterial, PointLight, Primitive, Shape,
+                    StratifiedSampler)
+from .transform import Transform
+
+_MUL = 6364136223846793005
+_MASK = (1 << 64) - 1
+
+
+def config_seed(config_index: int, scene_index: int = 0) -> int:
+    return 0x9E3779B9 ^ config_index ^ (scene_index << 8)
+
+
+class PCG32:
+    """PCG32 with vectorised draws.  ``uint32(n)`` returns the next n outputs."""
+
+    def __init__(self, seed: int, stream: int = 54):
+        self.inc = ((stream << 1) | 1) & _MASK
+        self.state = 0
+        self._step()
+        self.state = (self.state + seed) & _MASK
+        self._step()
+
+    def _step(self) -> None:
+        self.state = (self.state * _MUL + self.inc) & _MASK
+
+    @staticmethod
+    def _jump_tables(n: int, inc: int):
+        """A^k and C_k (k = 0..n-1) with s_k = A^k s_0 + C_k (mod 2^64)."""
+        a = np.empty(n, dtype=np.uint64)
+        c = np.empty(n, dtype=np.uint64)
+        ak, ck = 1, 0
+        for k in range(n):
+            a[k] = ak
+            c[k] = ck
+            ck = (ck * _MUL + inc) & _MASK
+            ak = (ak * _MUL) & _MASK
+        return a, c, ak, ck
+
+    def uint32(self, n: int) -> np.ndarray:
+        block = min(max(n, 1), 1 << 16)
+        a, c, ab, cb = self._jump_tables(block, self.inc)
+        out = np.empty(n, dtype=np.uint32)
+        s = self.state
+        pos = 0
+        with np.errstate(over="ignore"):
+            while pos < n:
+                m = min(block, n - pos)
+                st = a[:m] * np.uint64(s) + c[:m]  # states s_0 .. s_{m-1} (outputs use the old state)
+                xs = (((st >> np.uint64(18)) ^ st) >> np.uint64(27)).astype(np.uint32)
+                rot = (st >> np.uint64(59)).astype(np.uint32)
+                out[pos:pos + m] = (xs >> rot) | (xs << ((np.uint32(32) - rot) & np.uint32(31)))
+                pos += m
+                s = (ab * s + cb) & _MASK if m == block else (int(a[m - 1]) * s + int(c[m - 1])) * _MUL + self.inc
+                s &= _MASK
+        self.state = s
+        return out
+
+    def uniform(self, n: int) -> np.ndarray:
+        """n floats in [0, 1) as float64 (exact values of (u >> 8) * 2^-24)."""
+        return (self.uint32(n) >> np.uint32(8)).astype(np.float64) * (1.0 / 16777216.0)
+
+
+# ------------------------------------------------------------------ configs --
+def random_triangle_soup(rng: PCG32, n_tris: int, extent: float = 1.0, offset: float = 0.05,
+                         center=(0.0, 0.0, 0.0)) -> tuple[np.ndarray, np.ndarray]:
+    """n triangles: centroid U[-extent, extent]^3, vertices = centroid +
+    U[-offset, offset]^3 (12 draws per triangle, in that order)."""
+    u = rng.uniform(12 * n_tris).reshape(n_tris, 12)
+    cen = (u[:, 0:3] * 2.0 - 1.0) * extent + np.asarray(center, dtype=np.float64)
+    off = (u[:, 3:12].reshape(n_tris, 3, 3) * 2.0 - 1.0) * offset
+    pts = (cen[:, None, :] + off).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(3 * n_tris, dtype=np.uint32)
+    return pts, idx
+
+
+def rays_toward_center(rng: PCG32, n: int, radius: float = 3.0, target: float = 0.5,
+                       tmin: float = 1e-4, tmax: float = math.inf) -> np.ndarray:
+    """Origins uniform on a sphere of `radius`, directions normalised toward
+    a point uniform in [-target, target]^3 (5 draws per ray)."""
+    u = rng.uniform(5 * n).reshape(n, 5)
+    z = 1.0 - 2.0 * u[:, 0]
+    phi = 2.0 * math.pi * u[:, 1]
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    o = radius * np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    t = (u[:, 2:5] * 2.0 - 1.0) * target
+    d = t - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(n, dtype=abi.RAY_DTYPE)
+    rays["o"] = o.astype(np.float32)
+    rays["d"] = d.astype(np.float32)
+    rays["tmin"] = tmin
+    rays["tmax"] = tmax
+    return rays
+
+
+def incoherent_rays(rng: PCG32, n: int, lo, hi, tmin: float = 1e-4, tmax: float = math.inf) -> np.ndarray:
+    """Origins uniform in the box [lo, hi], directions uniform on the unit
+    sphere (5 draws per ray)."""
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    u = rng.uniform(5 * n).reshape(n, 5)
+    o = lo + u[:, 0:3] * (hi - lo)
+    z = 1.0 - 2.0 * u[:, 3]
+    phi = 2.0 * math.pi * u[:, 4]
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    d = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    rays = np.zeros(n, dtype=abi.RAY_DTYPE)
+    rays["o"] = o.astype(np.float32)
+    rays["d"] = d.astype(np.float32)
+    rays["tmin"] = tmin
+    rays["tmax"] = tmax
+    return rays
+
+
+def ray_soup(n_tris: int = 4096, n_rays: int = 1 << 20, seed: int | None = None):
+    """Plain ray-BVH queries: random triangle soup + rays toward the centre.
+    Returns (primitives, rays)."""
+    rng = PCG32(config_seed(0) if seed is None else seed)
+    pts, idx = random_triangle_soup(rng, n_tris)
+    mesh = Shape.triangle_mesh(Transform(), None, False, idx, pts)
+    rays = rays_toward_center(rng, n_rays)
+    return [Primitive.geometric(mesh)], rays
+
+
+def quad_light_mesh(center, size: float, facing_down: bool = True) -> Shape:
+    """A horizontal square of two triangles whose geometric normal (as the
+    reference computes it for refined triangles) points -y."""
+    cx, cy, cz = center
+    h = size / 2.0
+    A = (cx - h, cy, cz - h)
+    B = (cx + h, cy, cz - h)
+    Cc = (cx + h, cy, cz + h)
+    D = (cx - h, cy, cz + h)
+    pts = np.array([A, B, Cc, D], dtype=np.float32)
+    idx = np.array([0, 2, 1, 0, 3, 2] if facing_down else [0, 1, 2, 0, 2, 3], dtype=np.uint32)
+    return Shape.triangle_mesh(Transform(), None, False, idx, pts)
+
+
+POINT_LIGHT_POS = (0.0, 6.0, -2.0)
+
+
+def c1_scene(seed: int | None = None, res: int = 512, spp_side: int = 2, n_spheres: int = 64):
+    """Plain render: perspective camera at (0, 1.5, -6) looking at the
+    origin, fov 60; ground quad (2 triangles, y = 0, [-10, 10]^2); matte
+    spheres with r ~ U[0.1, 0.4], centre ~ U([-3,3] x [r,2] x [-3,3]),
+    Kd ~ U[0.2, 0.8]^3; a point light of intensity 50 at POINT_LIGHT_POS and
+    a 1x1 quad area light at y = 4 facing down with L = 10.
+    Returns (prims, lights, camera, sampler)."""
+    rng = PCG32(config_seed(1) if seed is None else seed)
+    prims = []
+    ground_pts = np.array([(-10, 0, -10), (10, 0, -10), (10, 0, 10), (-10, 0, 10)], np.float32)
+    ground = Shape.triangle_mesh(Transform(), None, False, np.array([0, 1, 2, 0, 2, 3], np.uint32), ground_pts)
+    prims.append(Primitive.geometric(ground, MatteMaterial((0.5, 0.5, 0.5))))
+    u = rng.uniform(7 * n_spheres).reshape(n_spheres, 7)
+    for i in range(n_spheres):
+        r = 0.1 + 0.3 * u[i, 0]
+        c = (-3.0 + 6.0 * u[i, 1], r + (2.0 - r) * u[i, 2], -3.0 + 6.0 * u[i, 3])
+        kd = tuple(0.2 + 0.6 * u[i, 4:7])
+        o2w = Transform.translate(c)
+        s = Shape.sphere(o2w, o2w.inverse(), False, r, -r, r, 360.0)
+        prims.append(Primitive.geometric(s, MatteMaterial(kd)))
+    lights = [PointLight(Transform.translate(POINT_LIGHT_POS), (50.0, 50.0, 50.0))]
+    area = DiffuseAreaLight(Transform(), (10.0, 10.0, 10.0))
+    prims.append(Primitive.geometric_area_light(quad_light_mesh((0.0, 4.0, 0.0), 1.0), MatteMaterial((0, 0, 0)),
+                                                area))
+    lights.append(area)
+    cam2world = Transform.look_at((0.0, 1.5, -6.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0)).inverse()
+    film = Film.image(res, res, Filter.mean(0.5, 0.5))
+    camera = Camera.perspective(cam2world, (-1.0, 1.0, -1.0, 1.0), 0.0, 1.0, 0.0, 1e30, 60.0, film)
+    sampler = StratifiedSampler.stratified(0, res, 0, res, spp_side, spp_side, True, 0.0, 1.0)
+    return prims, lights, camera, sampler
+
+
+def heightfield_points(n_side: int = 708, extent: float = 8.0, seed: int | None = None) -> tuple:
+    rng = PCG32(config_seed(2) if seed is None else seed)
+    ph = rng.uniform(12) * 2.0 * math.pi
+    xs = np.linspace(-extent, extent, n_side)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    H = np.zeros_like(X)
+    for k in range(1, 7):
+        H += 0.5 ** k * np.sin(2.0 ** k * X + ph[k - 1]) * np.cos(2.0 ** k * Z + ph[5 + k])
+    pts = np.stack([X, H, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+    i = np.arange(n_side - 1)
+    I, J = np.meshgrid(i, i, indexing="xy")
+    v00 = (J * n_side + I).reshape(-1)
+    v10 = v00 + 1
+    v01 = v00 + n_side
+    v11 = v01 + 1
+    idx = np.stack([v00, v01, v10, v10, v01, v11], axis=1).reshape(-1).astype(np.uint32)
+    return pts, idx, rng
+
+
+def heightfield(n_side: int = 708, seed: int | None = None, res: int = 1024, spp_side: int = 4,
+                n_rays: int = 1 << 22):
+    """Large mesh: 708x708-vertex heightfield over [-8, 8]^2 with
+    h = sum_k 0.5^k sin(2^k x + phi_k) cos(2^k z + psi_k), lit by a 4x4 quad
+    area light at y = 6 (L = 8); camera at (0, 7, -14) looking at the
+    origin, fov 50.  Returns (prims, lights, camera, sampler, rays); the
+    rays start uniformly in the mesh AABB inflated by 1 and point uniformly
+    over the sphere."""
+    pts, idx, rng = heightfield_points(n_side, 8.0, seed)
+    mesh = Shape.triangle_mesh(Transform(), None, False, idx, pts)
+    prims = [Primitive.geometric(mesh, MatteMaterial((0.55, 0.5, 0.45)))]
+    area = DiffuseAreaLight(Transform(), (8.0, 8.0, 8.0))
+    prims.append(Primitive.geometric_area_light(quad_light_mesh((0.0, 6.0, 0.0), 4.0), MatteMaterial((0, 0, 0)),
+                                                area))
+    lights = [area]
+    cam2world = Transform.look_at((0.0, 7.0, -14.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0)).inverse()
+    film = Film.image(res, res, Filter.mean(0.5, 0.5))
+    camera = Camera.perspective(cam2world, (-1.0, 1.0, -1.0, 1.0), 0.0, 1.0, 0.0, 1e30, 50.0, film)
+    sampler = StratifiedSampler.stratified(0, res, 0, res, spp_side, spp_side, True, 0.0, 1.0)
+    lo = pts.min(axis=0).astype(np.float64) - 1.0
+    hi = pts.max(axis=0).astype(np.float64) + 1.0
+    rays = incoherent_rays(rng, n_rays, lo, hi) if n_rays else None
+    return prims, lights, camera, sampler, rays

@@ -1,0 +1,98 @@
+"""The C-ABI library: it loads, exports every symbol the header declares, and
+its host-side parts (argument checks, BVH build, status strings) work
+without a GPU."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from pbrt_rust_gb300 import abi, generators as G
+from pbrt_rust_gb300.gpu import GpuBVHAccel
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "pbrt_gpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pbrtgpu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_expected_surface():
+    names = declared_functions()
+    for must in ("pbrtgpu_bvh_create", "pbrtgpu_intersect", "pbrtgpu_intersect_p", "pbrtgpu_render",
+                 "pbrtgpu_scene_create", "pbrtgpu_bvh_world_bound"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(abi.LIB_PATH)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (pbrtgpu_[a-z0-9_]+)", out))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    for n in declared_functions():
+        assert n in abi.SIGNATURES, f"{n} has no ctypes signature"
+        getattr(lib, n)
+
+
+def test_status_strings(lib):
+    assert lib.pbrtgpu_abi_version() == 1
+    assert lib.pbrtgpu_status_str(0) == b"ok"
+    assert lib.pbrtgpu_status_str(6) == b"traversal stack overflow"
+    assert lib.pbrtgpu_status_str(999) == b"unknown status"
+
+
+def test_invalid_arguments_fail_loudly(lib):
+    h = C.c_void_p()
+    assert lib.pbrtgpu_bvh_create(None, 3, 4, b"sah", C.byref(h)) == 1
+    assert b"NULL" in lib.pbrtgpu_last_error()
+    assert lib.pbrtgpu_intersect(None, None, 4, None, None) == 1
+    with pytest.raises(ValueError):
+        from pbrt_rust_gb300.scene import Shape
+        from pbrt_rust_gb300.transform import Transform
+        Shape.triangle_mesh(Transform(), None, False, [0, 1], np.zeros((3, 3)))
+
+
+def test_bad_mesh_index_is_rejected(lib):
+    d = abi.PbrtShapeDesc()
+    pts = np.zeros(9, np.float32)
+    idx = np.array([0, 1, 7], np.uint32)
+    d.kind = abi.SHAPE_TRIANGLE_MESH
+    d.object_to_world.m[:] = np.eye(4, dtype=np.float32).reshape(-1).tolist()
+    d.object_to_world.m_inv[:] = np.eye(4, dtype=np.float32).reshape(-1).tolist()
+    d.points = abi.f32p(pts)
+    d.n_points = 3
+    d.indices = abi.u32p(idx)
+    d.n_indices = 3
+    h = C.c_void_p()
+    assert lib.pbrtgpu_bvh_create(C.byref(d), 1, 4, b"sah", C.byref(h)) == 1  # PBRT_ERR_INVALID_ARGUMENT
+    assert b"out of range" in lib.pbrtgpu_last_error()
+
+
+def test_host_build_matches_oracle_on_cpu(lib, oracle):
+    """The product's BVH build (host side of pbrtgpu_bvh_create) equals the
+    oracle's restatement of BVHAccelerator::new node for node."""
+    prims, _ = G.ray_soup(3000, 1, seed=21)
+    for sm in ("sah", "middle", "equal"):
+        g = GpuBVHAccel(prims, 4, sm)
+        o = oracle.OracleBVH(prims, 4, sm)
+        assert np.array_equal(g.nodes().view(np.uint8), o.nodes().view(np.uint8))
+        assert np.array_equal(g.primitive_order(), o.primitive_order())
+        assert g.depth() == o.depth()
+
+
+def test_no_cpu_fallback_without_a_gpu(lib):
+    """Without a CUDA device the traversal fails with a status; it never
+    computes on the CPU."""
+    from conftest import HAS_GPU
+    if HAS_GPU:
+        pytest.skip("a GPU is present")
+    prims, rays = G.ray_soup(100, 16, seed=2)
+    g = GpuBVHAccel(prims)
+    with pytest.raises(abi.PbrtError) as e:
+        g.intersect(rays)
+    assert e.value.status in (2, 10)

@@ -1,0 +1,225 @@
+"""GPU parity of closest-hit and any-hit traversal against the CPU oracle.
+
+Tolerance: hit primitive indices bit-exact except where two hits lie within
+1e-6 * t; t within 1e-5 relative of an FP64 recomputation; any-hit
+booleans equal.  (The kernels repeat the reference's f32 arithmetic and
+visiting order, so in practice every field is bit-identical.)
+"""
+import math
+
+import numpy as np
+import pytest
+
+from pbrt_rust_gb300 import abi, generators as G
+from pbrt_rust_gb300.gpu import GpuBVHAccel
+from pbrt_rust_gb300.scene import Primitive, Shape
+from pbrt_rust_gb300.transform import Transform
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def to_dev(rays):
+    torch = _torch()
+    a = np.ascontiguousarray(rays).view(np.float32).reshape(-1, 8)
+    return torch.from_numpy(a.copy()).cuda()
+
+
+def dev_hits(bvh, rays):
+    torch = _torch()
+    out = bvh.intersect(to_dev(rays))
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(abi.HIT_DTYPE).reshape(-1)
+
+
+def dev_any(bvh, rays):
+    torch = _torch()
+    out = bvh.intersect_p(to_dev(rays))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def f64_t(tri, r):
+    """Moller-Trumbore in float64 for one triangle (p1, p2, p3) and ray."""
+    p1, p2, p3 = (tri[i].astype(np.float64) for i in range(3))
+    o = r["o"].astype(np.float64)
+    d = r["d"].astype(np.float64)
+    e1, e2 = p2 - p1, p3 - p1
+    s1 = np.cross(d, e2)
+    inv = 1.0 / np.dot(s1, e1)
+    s = o - p1
+    s2 = np.cross(s, e1)
+    return np.dot(e2, s2) * inv
+
+
+def assert_hits_match(oracle_bvh, got, want, rays, check_f64=True):
+    assert got.shape == want.shape
+    same_prim = got["prim"] == want["prim"]
+    if not np.all(same_prim):
+        bad = np.nonzero(~same_prim)[0]
+        for i in bad:  # allowed only for near-ties
+            assert got["prim"][i] >= 0 and want["prim"][i] >= 0, (i, got[i], want[i])
+            assert abs(got["t"][i] - want["t"][i]) <= 1e-6 * abs(want["t"][i]), (i, got[i], want[i])
+        assert len(bad) <= max(1, len(rays) // 100000)
+    hit = want["prim"] >= 0
+    ok = same_prim & hit
+    np.testing.assert_array_equal(got["t"][ok], want["t"][ok])
+    np.testing.assert_array_equal(got["b1"][ok], want["b1"][ok])
+    np.testing.assert_array_equal(got["b2"][ok], want["b2"][ok])
+    if check_f64:
+        idx = np.nonzero(ok)[0]
+        idx = idx[:: max(1, len(idx) // 500)]
+        for i in idx:
+            tri = oracle_bvh.triangle(int(got["prim"][i]))
+            t64 = f64_t(tri, rays[i])
+            assert abs(got["t"][i] - t64) <= 1e-5 * abs(t64), (i, got["t"][i], t64)
+
+
+@pytest.fixture(scope="module")
+def soup(oracle):
+    prims, rays = G.ray_soup(4096, 1 << 20)
+    gb = GpuBVHAccel(prims, 4, "sah")
+    ob = oracle.OracleBVH(prims, 4, "sah")
+    return prims, rays, gb, ob
+
+
+def test_ray_soup_closest_hit_matches_oracle(soup):
+    """4096 random triangles, 2^20 rays toward the centre (the plain ray-BVH
+    query workload)."""
+    prims, rays, gb, ob = soup
+    assert np.array_equal(gb.nodes().view(np.uint8), ob.nodes().view(np.uint8))
+    want = ob.intersect(rays)
+    got = dev_hits(gb, rays)
+    assert (want["prim"] >= 0).mean() > 0.3
+    assert_hits_match(ob, got, want, rays)
+
+
+def test_ray_soup_any_hit_matches_oracle(soup):
+    prims, rays, gb, ob = soup
+    np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
+
+
+def test_host_buffers_match_device_buffers(soup):
+    """The C ABI stages host buffers (numpy) through the device."""
+    prims, rays, gb, ob = soup
+    sub = rays[:50000]
+    host = gb.intersect(sub)
+    dev = dev_hits(gb, sub)
+    assert np.array_equal(host.view(np.uint8), dev.view(np.uint8))
+    np.testing.assert_array_equal(gb.intersect_p(sub), dev_any(gb, sub))
+
+
+def test_finite_tmax_and_tmin(soup, oracle):
+    """Segments (tmin > 0, finite tmax) as shadow rays use them."""
+    prims, rays, gb, ob = soup
+    r = rays[:200000].copy()
+    rng = np.random.default_rng(3)
+    r["tmin"] = rng.uniform(0.0, 2.0, len(r)).astype(np.float32)
+    r["tmax"] = (r["tmin"] + rng.uniform(0.0, 3.0, len(r))).astype(np.float32)
+    assert_hits_match(ob, dev_hits(gb, r), ob.intersect(r), r, check_f64=False)
+    np.testing.assert_array_equal(dev_any(gb, r), ob.intersect_p(r))
+
+
+@pytest.mark.parametrize("sm", ["middle", "equal"])
+def test_other_split_methods(oracle, sm):
+    prims, rays = G.ray_soup(2000, 1 << 16, seed=11)
+    gb = GpuBVHAccel(prims, 4, sm)
+    ob = oracle.OracleBVH(prims, 4, sm)
+    assert np.array_equal(gb.nodes().view(np.uint8), ob.nodes().view(np.uint8))
+    assert_hits_match(ob, dev_hits(gb, rays), ob.intersect(rays), rays)
+    np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
+
+
+def test_sphere_scene_matches_oracle(oracle):
+    """Triangles + 64 translated spheres + the area-light quad; random rays."""
+    prims, lights, cam, smp = G.c1_scene(res=64)
+    gb = GpuBVHAccel(prims, 4, "sah")
+    ob = oracle.OracleBVH(prims, 4, "sah")
+    rng = G.PCG32(99)
+    rays = G.incoherent_rays(rng, 1 << 18, (-4, 0, -4), (4, 3, 4))
+    want = ob.intersect(rays)
+    got = dev_hits(gb, rays)
+    assert (want["prim"] >= 1).sum() > 1000
+    assert_hits_match(ob, got, want, rays, check_f64=False)
+    np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
+
+
+def test_aggregate_kat_on_gpu(oracle):
+    """src/primitive/aggregates/mod.rs:93-138 through the device path."""
+    from test_kats import get_spheres, ray
+    rays = np.concatenate([ray((0, 0, -1), (0, 0, 1)), ray((-1, 0, 2), (1, 0, 0)), ray((4, 0, 0), (-2, 1, 1))])
+    for sm in ("sah", "middle", "equal"):
+        gb = GpuBVHAccel(get_spheres(), 1, sm)
+        assert dev_hits(gb, rays)["prim"].tolist() == [0, 4, 6]
+        assert gb.intersect(rays)["prim"].tolist() == [0, 4, 6]
+
+
+def test_tetrahedron_kat_on_gpu():
+    """src/primitive/aggregates/bvh.rs:457-488 through the device path."""
+    from test_kats import TET_PTS, TET_TRIS, ray
+    mesh = Shape.triangle_mesh(Transform(), None, False, TET_TRIS, TET_PTS)
+    for mp, sm in ((1, "sah"), (10, "middle")):
+        gb = GpuBVHAccel([mesh], mp, sm)
+        r = ray((0.25, -1.0, 0.25), (0.0, 1.0, 0.0))
+        assert dev_any(gb, r)[0] == 1
+        assert dev_hits(gb, r)["t"][0] == 1.0
+
+
+def test_partial_sphere_kats_on_gpu():
+    """src/shape/sphere.rs:209-264 as one-sphere aggregates on the device."""
+    from test_kats import ray
+    xf = Transform.translate((1.0, 2.0, 1.0))
+    full = GpuBVHAccel([Shape.sphere(xf, None, False, 1.0, -1.0, 1.0, 360.0)], 1, "sah")
+    dirs = [(1.0, 1.5, 1.0), (1.0, 1.0, 1.0), (1.0, 0.5, 1.0), (0.0, 2.0, 1.0), (1.0, 2.0, 0.0)]
+    rays = np.concatenate([ray((0, 0, 0), d) for d in dirs])
+    assert dev_any(full, rays).tolist() == [1, 1, 0, 1, 1]
+    xf2 = Transform.translate((0.0, -3.0, 0.0)) * Transform.scale(2.0, 2.0, 2.0)
+
+    def sph(z0, z1):
+        return GpuBVHAccel([Shape.sphere(xf2, None, False, 0.75, z0, z1, 180.0)], 1, "sah")
+
+    down = ray((0, 0, 0), (0, -1, 0))
+    assert dev_any(sph(-0.75, -0.5), down)[0] == 0
+    assert dev_any(sph(0.5, 0.75), down)[0] == 0
+    s2 = sph(-0.5, 0.75)
+    assert dev_hits(s2, down)["prim"][0] == 0
+    assert dev_any(s2, ray((0, -3, 0), (0, -1, 0)))[0] == 0
+    assert dev_any(s2, ray((0, -3, 0), (0, 1, 0)))[0] == 1
+    assert dev_any(s2, ray((0, -4, 10), (0, 0, -1)))[0] == 0
+
+
+def test_edge_cases(oracle):
+    """Empty batches, an empty aggregate, axis-aligned and degenerate rays."""
+    torch = _torch()
+    from test_kats import TET_PTS, TET_TRIS, ray
+    mesh = Shape.triangle_mesh(Transform(), None, False, TET_TRIS, TET_PTS)
+    gb = GpuBVHAccel([mesh], 1, "sah")
+    ob = oracle.OracleBVH([mesh], 1, "sah")
+    empty = np.zeros(0, dtype=abi.RAY_DTYPE)
+    assert gb.intersect(empty).shape == (0,)
+    assert gb.intersect_p(empty).shape == (0,)
+    none = GpuBVHAccel([], 4, "sah")
+    r = ray((0, 0, 0), (1, 1, 1))
+    assert none.intersect(r)["prim"][0] == -1 and none.intersect_p(r)[0] == 0
+    lo, hi = none.world_bound()
+    assert lo[0] == np.finfo(np.float32).max and hi[0] == -np.finfo(np.float32).max
+    cases = [ray((0.25, -1, 0.25), (0, 1, 0)), ray((-1, 0.25, 0.25), (1, 0, 0)), ray((0.25, 0.25, -1), (0, 0, 1)),
+             ray((0.25, 0.25, 5), (0, 0, -1)), ray((0, 0, 0), (0, 0, 0)), ray((0.2, 0.2, 0.2), (1, 0, 0)),
+             ray((0.25, -1, 0.25), (0, 1, 0), 2.0, 1.0), ray((0.25, -1, 0.25), (-0.0, 1, -0.0)),
+             ray((0, 0, 0), (1, 1, 1), 0.0, float("inf")), ray((1, 0, 0), (-1, 1, 0))]
+    rays = np.concatenate(cases)
+    want = ob.intersect(rays, nthreads=1)
+    got = dev_hits(gb, rays)
+    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays, nthreads=1))
+    assert torch.cuda.is_available()
+
+
+def test_world_bound_matches_oracle(soup):
+    prims, rays, gb, ob = soup
+    for a, b in zip(gb.world_bound(), ob.world_bound()):
+        assert np.array_equal(a, b)
