@@ -252,6 +252,8 @@ def run_ours(args):
         ms_closest = timed(closest, args.steps, args.warmup)
     ms_any = timed(anyhit, max(3, args.steps // 2), args.warmup)
 
+    print(f"[bench] closest {statistics.mean(ms_closest):.3f} ms/step, any {statistics.mean(ms_any):.3f} ms/step",
+          file=sys.stderr, flush=True)
     # e2e: pinned host buffers through the C ABI (copies inside the step)
     rays_host = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
     hits_host = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
@@ -266,7 +268,7 @@ def run_ours(args):
     e2e_mrays = N_RAYS / statistics.mean(e2e_t) / 1e6
     # the host copy of the result must equal the device-resident one
     torch.cuda.synchronize(dev)
-    if not torch.equal(hits_host, hits_dev.cpu()):
+    if not torch.equal(hits_host.view(torch.int32), hits_dev.cpu().view(torch.int32)):
         raise RuntimeError("host-buffer and device-buffer hits differ")
 
     # render of the same scene: 1024x1024, 16 spp, direct lighting

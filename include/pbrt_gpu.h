@@ -170,9 +170,10 @@ const char* pbrtgpu_last_error(void);
  * (src/primitive/aggregates/bvh.rs:334-363) and Aggregate::bvh
  * (src/primitive/aggregates/mod.rs:27-29).  The primitives are fully
  * refined, the SAH/middle/equal tree is built on the host with the
- * reference's arithmetic, flattened, and uploaded to the current device.
+ * reference's arithmetic and flattened.
  * An unknown split_method falls back to "sah" with a warning, as
- * bvh.rs:341-349 does. */
+ * bvh.rs:341-349 does.  The device copy is made on the then-current
+ * device by the first call that needs it (intersect or render). */
 int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
                        uint32_t max_prims_in_node, const char* split_method,
                        PbrtBVH** out);
@@ -203,6 +204,24 @@ int pbrtgpu_intersect(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
  * BVH: occluded[i] = 1 if any primitive is hit within [tmin, tmax]. */
 int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
                         uint8_t* occluded, void* stream);
+
+/* Traversal kernel choice (process-wide), set by the autotuner.  Every
+ * kernel visits the reference's tree in the reference's order, so results
+ * do not depend on the choice.  The first value is also read from the
+ * environment (PBRT_TRACE_KERNEL = plain | pt | w4 | w4pt,
+ * PBRT_TRACE_REFILL = 1..32) when no call has set it. */
+enum {
+    PBRT_TRACE_PAIR = 0,            /* binary pairs, one thread per ray */
+    PBRT_TRACE_PAIR_PERSISTENT = 1, /* binary pairs, persistent warps */
+    PBRT_TRACE_WIDE = 2,            /* 4-wide nodes, one thread per ray */
+    PBRT_TRACE_WIDE_PERSISTENT = 3  /* 4-wide nodes, persistent warps */
+};
+typedef struct PbrtTraceConfig {
+    int32_t kernel;   /* PBRT_TRACE_* */
+    uint32_t refill;  /* persistent kernels: refill a warp when this many lanes idle */
+} PbrtTraceConfig;
+int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg);
+int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg);
 
 /* ---- renderer: the GpuSamplerRenderer drop-in ------------------------- */
 

@@ -91,6 +91,13 @@ class PbrtSamplerDesc(C.Structure):
     ]
 
 
+class PbrtTraceConfig(C.Structure):
+    _fields_ = [("kernel", C.c_int32), ("refill", C.c_uint32)]
+
+
+TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3}
+
+
 class PbrtPackedNode(C.Structure):
     _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("is_leaf", C.c_int32), ("offset", C.c_uint32),
                 ("count", C.c_uint32)]
@@ -119,6 +126,8 @@ SIGNATURES = {
     "pbrtgpu_bvh_get_primitive_order": (C.c_int, [_P, _U32P, C.c_uint32]),
     "pbrtgpu_intersect": (C.c_int, [_P, _P, C.c_uint32, _P, _P]),
     "pbrtgpu_intersect_p": (C.c_int, [_P, _P, C.c_uint32, _P, _P]),
+    "pbrtgpu_set_trace_config": (C.c_int, [C.POINTER(PbrtTraceConfig)]),
+    "pbrtgpu_get_trace_config": (C.c_int, [C.POINTER(PbrtTraceConfig)]),
     "pbrtgpu_scene_create": (C.c_int, [C.POINTER(PbrtSceneDesc), C.POINTER(_P)]),
     "pbrtgpu_scene_destroy": (None, [_P]),
     "pbrtgpu_scene_bvh": (C.c_int, [_P, C.POINTER(_P)]),
@@ -149,6 +158,21 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     if path is None:
         _lib = lib
     return lib
+
+
+def set_trace_kernel(kernel: str, refill: int = 8) -> None:
+    """Choose the traversal kernel: 'plain', 'pt', 'w4' or 'w4pt'."""
+    lib = load()
+    cfg = PbrtTraceConfig(TRACE_KERNELS[kernel], refill)
+    check(lib.pbrtgpu_set_trace_config(C.byref(cfg)), lib)
+
+
+def get_trace_kernel() -> tuple[str, int]:
+    lib = load()
+    cfg = PbrtTraceConfig()
+    check(lib.pbrtgpu_get_trace_config(C.byref(cfg)), lib)
+    names = {v: k for k, v in TRACE_KERNELS.items()}
+    return names[cfg.kernel], cfg.refill
 
 
 def check(status: int, lib: C.CDLL | None = None) -> None:

@@ -87,6 +87,7 @@ int bvh_upload(PbrtBVH* b) {
     if ((st = upload(&b->d_pairs, b->host.pairs))) return st;
     if ((st = upload(&b->d_prims, b->host.recs))) return st;
     if ((st = upload(&b->d_spheres, b->host.spheres))) return st;
+    if ((st = upload(&b->d_nodes4, b->host.nodes4))) return st;
     if ((st = cuda_status(cudaMalloc(&b->d_status, sizeof(int)), "cudaMalloc"))) return st;
     if ((st = cuda_status(cudaMemset(b->d_status, 0, sizeof(int)), "cudaMemset"))) return st;
     b->dev.pairs = b->d_pairs;
@@ -96,8 +97,18 @@ int bvh_upload(PbrtBVH* b) {
     b->dev.has_spheres = b->host.has_spheres ? 1u : 0u;
     b->dev.n_prims = (uint32_t)b->host.recs.size();
     b->dev.empty = b->host.nodes.empty() ? 1u : 0u;
+    b->dev4.nodes = b->d_nodes4;
+    b->dev4.prims = b->d_prims;
+    b->dev4.spheres = b->d_spheres;
+    b->dev4.root = b->host.root4;
+    b->dev4.empty = b->dev.empty;
     b->uploaded = true;
     return PBRT_OK;
+}
+
+// The 4-wide layout when a compiled variant covers its stack bound.
+const DevBVH4* wide_of(const PbrtBVH* b) {
+    return wide_stack_variant(b->host.stack4_bound) ? &b->dev4 : nullptr;
 }
 
 // Runs closest/any hit for host or device buffers.
@@ -115,7 +126,9 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
     size_t out_bytes = hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n;
     bool dr = is_device_pointer(rays), dout = is_device_pointer(out);
     if (dr && dout)
-        return cuda_status(launch_trace(b->dev, b->host.depth, rays, n, hits, occ, b->d_status, s), "trace launch");
+        return cuda_status(launch_trace(b->dev, b->host.depth, rays, n, hits, occ, b->d_status, s, wide_of(b),
+                                        b->host.stack4_bound),
+                           "trace launch");
     std::lock_guard<std::mutex> lk(b->stage_mu);
     const PbrtRay* d_rays = rays;
     if (!dr) {
@@ -132,7 +145,8 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
         d_out = b->stage_out.p;
     }
     if ((st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, hits ? (PbrtHit*)d_out : nullptr,
-                                       hits ? nullptr : (uint8_t*)d_out, b->d_status, s),
+                                       hits ? nullptr : (uint8_t*)d_out, b->d_status, s, wide_of(b),
+                                       b->host.stack4_bound),
                           "trace launch")))
         return st;
     if (!dout &&
@@ -155,6 +169,7 @@ PbrtBVH::~PbrtBVH() {
     if (d_pairs) cudaFree(d_pairs);
     if (d_prims) cudaFree(d_prims);
     if (d_spheres) cudaFree(d_spheres);
+    if (d_nodes4) cudaFree(d_nodes4);
     if (d_status) cudaFree(d_status);
     stage_in.release();
     stage_out.release();
@@ -259,6 +274,22 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t ca
     if (!b || (!out && !b->host.ordered.empty())) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (cap < b->host.ordered.size()) return set_error(PBRT_ERR_INVALID_ARGUMENT, "capacity too small");
     if (!b->host.ordered.empty()) std::memcpy(out, b->host.ordered.data(), b->host.ordered.size() * sizeof(uint32_t));
+    return PBRT_OK;
+}
+
+int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg) {
+    if (!cfg || set_trace_config(cfg->kernel, cfg->refill))
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "trace config: kernel must be 0..3 and refill 1..32");
+    return PBRT_OK;
+}
+
+int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg) {
+    if (!cfg) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    int k;
+    unsigned r;
+    get_trace_config(&k, &r);
+    cfg->kernel = k;
+    cfg->refill = r;
     return PBRT_OK;
 }
 

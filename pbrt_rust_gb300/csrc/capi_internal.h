@@ -9,6 +9,7 @@
 #include "../../include/pbrt_gpu.h"
 #include "host_scene.h"
 #include "trace.cuh"
+#include "trace4.cuh"
 
 namespace pbrt {
 
@@ -39,8 +40,10 @@ struct PbrtBVH {
     pbrt::NodePair* d_pairs = nullptr;
     pbrt::PrimRec* d_prims = nullptr;
     pbrt::SphereRec* d_spheres = nullptr;
+    pbrt::Node4* d_nodes4 = nullptr;
     int* d_status = nullptr;
     pbrt::DevBVH dev{};
+    pbrt::DevBVH4 dev4{};
     std::mutex stage_mu;
     std::mutex upload_mu;
     std::atomic<bool> uploaded{false};  // device copy made by the first call that needs it
@@ -50,4 +53,5 @@ struct PbrtBVH {
 
 namespace pbrt {
 int bvh_upload(PbrtBVH* b);
+const DevBVH4* wide_of(const PbrtBVH* b);
 }

@@ -418,6 +418,9 @@ int pbrtgpu_render(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSam
     P.n_tasks = smp->num_tasks;
     P.bvh = S->bvh->dev;
     P.depth = S->bvh->host.depth;
+    P.bvh4 = S->bvh->dev4;
+    P.wide_bound = S->bvh->host.stack4_bound;
+    P.has_wide = wide_of(S->bvh) ? 1u : 0u;
     P.shade = S->d_shade;
     P.spheres = S->bvh->d_spheres;
     P.materials = S->d_materials;

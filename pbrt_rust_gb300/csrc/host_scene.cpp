@@ -436,6 +436,90 @@ static void fill_device_layout(HostBVH& H) {
     }
 }
 
+// Collapse the binary tree two levels at a time (see layout.h: Node4) and
+// mark the last primitive of every leaf.
+static void fill_node4_layout(HostBVH& H) {
+    const size_t m = H.nodes.size();
+    H.nodes4.clear();
+    H.stack4_bound = 0;
+    for (size_t k = 0; k < m; ++k) {
+        const FlatNode& nd = H.nodes[k];
+        if (nd.leaf && nd.count > 0) {
+            uint32_t last = nd.offset + nd.count - 1;
+            uint32_t flag = kPrimLastBit;
+            std::memcpy(&H.recs[last].r2[3], &flag, 4);
+        }
+    }
+    if (m == 0) return;
+    auto box_rec = [&](size_t k, ChildRec& c) {
+        const FlatNode& nd = H.nodes[k];
+        c.lo_x = nd.box.lo.x;
+        c.lo_y = nd.box.lo.y;
+        c.lo_z = nd.box.lo.z;
+        c.hi_x = nd.box.hi.x;
+        c.hi_y = nd.box.hi.y;
+        c.hi_z = nd.box.hi.z;
+    };
+    // index of the Node4 rooted at each binary inner node that starts one
+    std::vector<uint32_t> n4_of(m, kNode4Empty);
+    // pre-order walk: a binary inner node reached as a grandchild (or the
+    // root) starts a Node4
+    struct Item {
+        size_t k;
+        uint32_t pushes;  // stack entries the traversal may hold above it
+    };
+    std::vector<Item> todo{{0, 0}};
+    std::vector<size_t> order;
+    while (!todo.empty()) {
+        Item it = todo.back();
+        todo.pop_back();
+        const FlatNode& N = H.nodes[it.k];
+        if (N.leaf) continue;
+        n4_of[it.k] = (uint32_t)order.size();
+        order.push_back(it.k);
+        size_t L = it.k + 1, R = N.offset;
+        size_t kids[4] = {SIZE_MAX, SIZE_MAX, SIZE_MAX, SIZE_MAX};
+        if (H.nodes[L].leaf) kids[0] = L; else { kids[0] = L + 1; kids[1] = H.nodes[L].offset; }
+        if (H.nodes[R].leaf) kids[2] = R; else { kids[2] = R + 1; kids[3] = H.nodes[R].offset; }
+        uint32_t nk = 0;
+        for (size_t kk : kids) nk += kk != SIZE_MAX;
+        uint32_t here = it.pushes + nk - 1;
+        H.stack4_bound = std::max(H.stack4_bound, here);
+        for (int s = 3; s >= 0; --s)
+            if (kids[s] != SIZE_MAX && !H.nodes[kids[s]].leaf) todo.push_back({kids[s], here});
+    }
+    H.nodes4.assign(order.size(), Node4{});
+    for (size_t i = 0; i < order.size(); ++i) {
+        size_t k = order[i];
+        const FlatNode& N = H.nodes[k];
+        size_t L = k + 1, R = N.offset;
+        size_t kids[4] = {SIZE_MAX, SIZE_MAX, SIZE_MAX, SIZE_MAX};
+        uint32_t axL = 0, axR = 0;
+        if (H.nodes[L].leaf) kids[0] = L; else { kids[0] = L + 1; kids[1] = H.nodes[L].offset; axL = H.nodes[L].count; }
+        if (H.nodes[R].leaf) kids[2] = R; else { kids[2] = R + 1; kids[3] = H.nodes[R].offset; axR = H.nodes[R].count; }
+        Node4& n4 = H.nodes4[i];
+        for (int s = 0; s < 4; ++s) {
+            ChildRec& c = n4.c[s];
+            if (kids[s] == SIZE_MAX) {
+                c.lo_x = c.lo_y = c.lo_z = FLT_MAX;
+                c.hi_x = c.hi_y = c.hi_z = -FLT_MAX;
+                c.a = kNode4Empty;
+            } else {
+                box_rec(kids[s], c);
+                const FlatNode& G = H.nodes[kids[s]];
+                c.a = G.leaf ? (kNode4Leaf | G.offset) : n4_of[kids[s]];
+            }
+            c.b = 0;
+        }
+        n4.c[0].b = N.count | (axL << 2) | (axR << 4);
+    }
+    ChildRec r;
+    box_rec(0, r);
+    r.a = H.nodes[0].leaf ? (kNode4Leaf | H.nodes[0].offset) : 0u;
+    r.b = 0;
+    H.root4 = r;
+}
+
 int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
                    HostBVH* out, std::string* err) {
     HostBVH& H = *out;
@@ -510,6 +594,7 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
     int st = build_tree(H, max_prims, parse_split_method(split_method), err);
     if (st) return st;
     fill_device_layout(H);
+    fill_node4_layout(H);
     return PBRT_OK;
 }
 

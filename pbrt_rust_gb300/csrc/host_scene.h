@@ -89,6 +89,10 @@ struct HostBVH {
     std::vector<NodePair> pairs;
     std::vector<PrimRec> recs;
     bool has_spheres = false;
+    // 4-wide layout (same tree, two binary levels per node)
+    ChildRec root4{};
+    std::vector<Node4> nodes4;
+    uint32_t stack4_bound = 0;  // most entries a 4-wide traversal can push
 };
 
 // Fully refine shapes, build and flatten the BVH, and fill the device

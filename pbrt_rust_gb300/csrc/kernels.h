@@ -5,6 +5,7 @@
 
 #include "../../include/pbrt_gpu.h"
 #include "trace.cuh"
+#include "trace4.cuh"
 
 namespace pbrt {
 
@@ -15,7 +16,14 @@ int trace_stack_for_depth(uint32_t depth);
 // Closest hit into `hits` (occluded == nullptr) or any hit into `occluded`.
 // All pointers are device pointers; d_status receives a PbrtStatus > 0 on a
 // device-side failure.
+// `wide` (may be null) selects the 4-wide layout with the given stack bound.
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
-                         uint8_t* occluded, int* d_status, cudaStream_t stream);
+                         uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide = nullptr,
+                         uint32_t wide_bound = 0);
+// Process-wide traversal kernel choice (PBRT_TRACE_*); 0 on success.
+int set_trace_config(int kernel, unsigned refill);
+void get_trace_config(int* kernel, unsigned* refill);
+// 64 or 256 when a compiled 4-wide variant covers this stack bound, else 0.
+int wide_stack_variant(uint32_t bound);
 
 }  // namespace pbrt

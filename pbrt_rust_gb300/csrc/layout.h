@@ -37,12 +37,29 @@ static_assert(sizeof(NodePair) == 64, "node pair is 64 bytes");
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kCountMask = 0x7fffffffu;
 
+// 4-wide node collapsed from two levels of the reference's binary tree.
+// For a binary inner node N with children L (first) and R (second):
+//   slot 0/1 = L's first/second child (slot 0 = L itself if L is a leaf,
+//   slot 1 then empty), slot 2/3 = the same for R.
+// Child record words: a = kNode4Leaf | first primitive, or the index of
+// the child's own Node4, or kNode4Empty; b of slot 0 holds the node's
+// three binary split axes: axis(N) | axis(L) << 2 | axis(R) << 4.
+// The primitives of a leaf child end at the record that carries
+// kPrimLastBit (PrimRec r2[3]).
+struct alignas(128) Node4 {
+    ChildRec c[4];
+};
+static_assert(sizeof(Node4) == 128, "4-wide node is 128 bytes");
+constexpr uint32_t kNode4Leaf = 0x80000000u;
+constexpr uint32_t kNode4Empty = 0xffffffffu;
+constexpr uint32_t kPrimLastBit = 1u;
+
 // 48-byte primitive record in BVH (ordered) order.  Triangle: p1 and the
 // edges e1 = p2 - p1, e2 = p3 - p1, computed on the host with the same f32
 // subtraction the reference does per test (src/shape/mesh.rs:45-46).
 //   r0 = (p1.xyz, id)  id = refined input index | kSphereBit if a sphere
 //   r1 = (e1.xyz, sphere index bits for spheres)
-//   r2 = (e2.xyz, 0)
+//   r2 = (e2.xyz, flags: kPrimLastBit on the last primitive of a leaf)
 struct alignas(16) PrimRec {
     float r0[4];
     float r1[4];

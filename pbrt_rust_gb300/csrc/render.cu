@@ -364,6 +364,22 @@ __global__ void __launch_bounds__(128) k_shadow(RenderParams P) {
     P.occluded[P.shadow_slot[q]] = occ ? 1 : 0;
 }
 
+template <int SMAX, int OVF>
+__global__ void __launch_bounds__(128) k_shadow4(RenderParams P) {
+    extern __shared__ uint2 smem_stack[];
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= *(volatile uint32_t*)&P.counters[0]) return;
+    const float4* r4 = reinterpret_cast<const float4*>(P.shadow_rays);
+    DRay r = make_dray(r4[2 * (size_t)q], r4[2 * (size_t)q + 1]);
+    Traversal4<SMAX, OVF> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    if (T.start(P.bvh4, r))
+        while (T.template step<true>(P.bvh4, r)) {
+        }
+    if (T.overflow) atomicMax((int*)&P.counters[2], 6);
+    P.occluded[P.shadow_slot[q]] = T.found ? 1 : 0;
+}
+
 // --------------------------------------------------------------- combine ---
 __global__ void __launch_bounds__(256) k_combine(RenderParams P) {
     const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -470,13 +486,19 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
     }
     if (P.n_samples) {
         e = launch_trace(P.bvh, P.depth, P.rays, (uint32_t)P.n_samples, reinterpret_cast<PbrtHit*>(P.hits), nullptr,
-                         (int*)&P.counters[2], s);
+                         (int*)&P.counters[2], s, P.has_wide ? &P.bvh4 : nullptr, P.wide_bound);
         if (e != cudaSuccess) return e;
         k_shade<<<blocks_for(P.n_samples, 128), 128, 0, s>>>(P);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         uint64_t max_shadow = P.n_samples * P.n_lights;
         if (max_shadow) {
-            if (trace_stack_for_depth(P.depth) == 64)
+            const size_t smem = 16 * sizeof(uint2) * 128;
+            int wv = P.has_wide ? wide_stack_variant(P.wide_bound) : 0;
+            if (wv == 64)
+                k_shadow4<16, 48><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
+            else if (wv == 256)
+                k_shadow4<16, 240><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
+            else if (trace_stack_for_depth(P.depth) == 64)
                 k_shadow<64><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
             else
                 k_shadow<256><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);

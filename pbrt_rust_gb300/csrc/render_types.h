@@ -4,6 +4,7 @@
 
 #include "layout.h"
 #include "trace.cuh"
+#include "trace4.cuh"
 
 namespace pbrt {
 
@@ -66,6 +67,9 @@ struct RenderParams {
     // scene
     DevBVH bvh;
     uint32_t depth;
+    DevBVH4 bvh4;
+    uint32_t wide_bound;  // 4-wide stack bound; wide layout used when has_wide
+    uint32_t has_wide;
     const ShadePrim* shade;
     const SphereRec* spheres;
     const float4* materials;     // kd.rgb (clamped >= 0), sigma

@@ -1,9 +1,13 @@
 // trace.cu - batched closest-hit / any-hit kernels over PbrtRay arrays.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include "../../include/pbrt_gpu.h"
 #include "kernels.h"
 #include "trace.cuh"
+#include "trace4.cuh"
 
 namespace pbrt {
 
@@ -27,6 +31,223 @@ __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restr
         hits[i] = make_float4(__int_as_float(res.prim), res.t, res.b1, res.b2);
 }
 
+// Persistent warps: the grid holds exactly the resident warps; each warp
+// owns a contiguous range of rays and, whenever at least REFILL of its
+// lanes are idle, hands them the next rays of its range.  Rays of very
+// different lengths then share warps without leaving lanes idle until the
+// longest one finishes.  Each ray's own traversal is unchanged, so results
+// are identical to k_trace.
+template <int STACK, bool ANY>
+__global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
+                                                          float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                          int* __restrict__ status, uint32_t per_warp,
+                                                          uint32_t refill) {
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t next = warp * per_warp;
+    const uint64_t end = (next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n;
+    const uint32_t kNone = 0xffffffffu;
+    uint32_t ray = kNone;
+    int st = 0;
+    DRay r;
+    Traversal<STACK> T;
+    auto finish = [&]() {
+        if (ANY)
+            occ[ray] = T.found ? 1 : 0;
+        else
+            hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        ray = kNone;
+    };
+    for (;;) {
+        unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
+        unsigned nidle = __popc(idle);
+        if (next < end && nidle >= (next + nidle >= end ? 1u : refill)) {
+            if (ray == kNone) {
+                uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
+                if (my < end) {
+                    ray = (uint32_t)my;
+                    r = make_dray(__ldg(rays + 2 * my), __ldg(rays + 2 * my + 1));
+                    if (!T.start(bvh, r)) finish();
+                }
+            }
+            next += nidle;
+        }
+        bool busy = ray != kNone;
+        if (!__any_sync(0xffffffffu, busy)) {
+            if (next >= end) break;
+            continue;
+        }
+        if (busy && !T.template step<ANY>(bvh, r, &st)) finish();
+    }
+    if (st) atomicMax(status, st);
+}
+
+// 4-wide traversal, one thread per ray.
+template <int SMAX, int OVF, bool ANY>
+__global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
+                                                float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                int* __restrict__ status) {
+    extern __shared__ uint2 smem_stack[];
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    DRay r = make_dray(__ldg(rays + 2 * (size_t)i), __ldg(rays + 2 * (size_t)i + 1));
+    Traversal4<SMAX, OVF> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    if (T.start(bvh, r))
+        while (T.template step<ANY>(bvh, r)) {
+        }
+    if (T.overflow) atomicMax(status, 6);
+    if (ANY)
+        occ[i] = T.found ? 1 : 0;
+    else
+        hits[i] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+}
+
+// 4-wide traversal with persistent warps refilling idle lanes (see
+// k_trace_persistent).
+template <int SMAX, int OVF, bool ANY>
+__global__ void __launch_bounds__(128) k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
+                                                           float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                           int* __restrict__ status, uint32_t per_warp,
+                                                           uint32_t refill) {
+    extern __shared__ uint2 smem_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t next = warp * per_warp;
+    const uint64_t end = (next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n;
+    const uint32_t kNone = 0xffffffffu;
+    uint32_t ray = kNone;
+    bool overflow = false;
+    DRay r;
+    Traversal4<SMAX, OVF> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    for (;;) {
+        unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
+        unsigned nidle = __popc(idle);
+        if (next < end && nidle >= (next + nidle >= end ? 1u : refill)) {
+            if (ray == kNone) {
+                uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
+                if (my < end) {
+                    ray = (uint32_t)my;
+                    r = make_dray(__ldg(rays + 2 * my), __ldg(rays + 2 * my + 1));
+                    bool live = T.start(bvh, r);
+                    if (!live) {
+                        if (ANY)
+                            occ[ray] = 0;
+                        else
+                            hits[ray] = make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f);
+                        ray = kNone;
+                    }
+                }
+            }
+            next += nidle;
+        }
+        bool busy = ray != kNone;
+        if (!__any_sync(0xffffffffu, busy)) {
+            if (next >= end) break;
+            continue;
+        }
+        if (busy && !T.template step<ANY>(bvh, r)) {
+            overflow |= T.overflow;
+            if (ANY)
+                occ[ray] = T.found ? 1 : 0;
+            else
+                hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+            ray = kNone;
+        }
+    }
+    if (overflow) atomicMax(status, 6);
+}
+
+enum { kVariantPairPlain = 0, kVariantPairPersistent = 1, kVariantWidePlain = 2, kVariantWidePersistent = 3 };
+static int g_kernel_variant = -1;
+static unsigned g_refill = 4;
+
+static void read_variant() {
+    if (g_kernel_variant >= 0) return;
+    g_kernel_variant = kVariantWidePersistent;
+    if (const char* v = getenv("PBRT_TRACE_KERNEL")) {
+        if (!strcmp(v, "plain")) g_kernel_variant = kVariantPairPlain;
+        else if (!strcmp(v, "pt")) g_kernel_variant = kVariantPairPersistent;
+        else if (!strcmp(v, "w4")) g_kernel_variant = kVariantWidePlain;
+        else if (!strcmp(v, "w4pt")) g_kernel_variant = kVariantWidePersistent;
+    }
+    if (const char* r = getenv("PBRT_TRACE_REFILL")) {
+        int x = atoi(r);
+        if (x >= 1 && x <= 32) g_refill = (unsigned)x;
+    }
+}
+
+template <int SMAX, int OVF, bool ANY>
+static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
+                               int* d_status, cudaStream_t stream, bool persistent) {
+    const int block = 128;
+    const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
+    if (!persistent) {
+        unsigned grid = (unsigned)((n + block - 1) / block);
+        k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status);
+        return cudaGetLastError();
+    }
+    static int bps = 0, sms = 0;
+    if (bps == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY>, block, smem);
+        if (bps < 1) bps = 1;
+    }
+    uint64_t warps = (uint64_t)sms * bps * (block / 32);
+    uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
+    if (per_warp < 32) per_warp = 32;
+    uint64_t need_warps = (n + per_warp - 1) / per_warp;
+    unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
+    k_trace4_persistent<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status, per_warp,
+                                                                      g_refill);
+    return cudaGetLastError();
+}
+
+int set_trace_config(int kernel, unsigned refill) {
+    if (kernel < kVariantPairPlain || kernel > kVariantWidePersistent || refill < 1 || refill > 32) return 1;
+    read_variant();
+    g_kernel_variant = kernel;
+    g_refill = refill;
+    return 0;
+}
+void get_trace_config(int* kernel, unsigned* refill) {
+    read_variant();
+    *kernel = g_kernel_variant;
+    *refill = g_refill;
+}
+
+int wide_stack_variant(uint32_t bound) {
+    if (bound <= 64) return 64;
+    if (bound <= 256) return 256;
+    return 0;
+}
+
+template <int STACK, bool ANY>
+static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
+                                     int* d_status, cudaStream_t stream) {
+    static int blocks_per_sm[2][2] = {{0, 0}, {0, 0}};
+    static int sms = 0;
+    const int block = 128;
+    int& bps = blocks_per_sm[STACK == 256][ANY];
+    if (bps == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace_persistent<STACK, ANY>, block, 0);
+        if (bps < 1) bps = 1;
+    }
+    uint64_t warps = (uint64_t)sms * bps * (block / 32);
+    uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
+    if (per_warp < 32) per_warp = 32;
+    uint64_t need_warps = (n + per_warp - 1) / per_warp;
+    unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
+    k_trace_persistent<STACK, ANY><<<grid, block, 0, stream>>>(bvh, r4, n, h4, occ, d_status, per_warp, g_refill);
+    return cudaGetLastError();
+}
+
 int trace_stack_for_depth(uint32_t depth) {
     if (depth <= 64) return 64;
     if (depth <= 256) return 256;
@@ -34,14 +255,37 @@ int trace_stack_for_depth(uint32_t depth) {
 }
 
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
-                         uint8_t* occluded, int* d_status, cudaStream_t stream) {
+                         uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
+                         uint32_t wide_bound) {
     if (n == 0) return cudaSuccess;
+    read_variant();
+    if (wide && (g_kernel_variant == kVariantWidePlain || g_kernel_variant == kVariantWidePersistent)) {
+        const float4* r4 = reinterpret_cast<const float4*>(rays);
+        float4* h4 = reinterpret_cast<float4*>(hits);
+        const bool any = occluded != nullptr, pt = g_kernel_variant == kVariantWidePersistent;
+        int v = wide_stack_variant(wide_bound);
+        if (v == 64)
+            return any ? launch_wide<16, 48, true>(*wide, r4, n, nullptr, occluded, d_status, stream, pt)
+                       : launch_wide<16, 48, false>(*wide, r4, n, h4, nullptr, d_status, stream, pt);
+        if (v == 256)
+            return any ? launch_wide<16, 240, true>(*wide, r4, n, nullptr, occluded, d_status, stream, pt)
+                       : launch_wide<16, 240, false>(*wide, r4, n, h4, nullptr, d_status, stream, pt);
+    }
     const int block = 128;
     const unsigned grid = (unsigned)((n + block - 1) / block);
     const float4* r4 = reinterpret_cast<const float4*>(rays);
     float4* h4 = reinterpret_cast<float4*>(hits);
     int stack = trace_stack_for_depth(depth);
     bool any = occluded != nullptr;
+    if (g_kernel_variant == kVariantPairPersistent) {
+        if (stack == 64)
+            return any ? launch_persistent<64, true>(bvh, r4, n, nullptr, occluded, d_status, stream)
+                       : launch_persistent<64, false>(bvh, r4, n, h4, nullptr, d_status, stream);
+        if (stack == 256)
+            return any ? launch_persistent<256, true>(bvh, r4, n, nullptr, occluded, d_status, stream)
+                       : launch_persistent<256, false>(bvh, r4, n, h4, nullptr, d_status, stream);
+        return cudaErrorInvalidValue;
+    }
     if (stack == 64) {
         if (any)
             k_trace<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, nullptr, occluded, d_status);

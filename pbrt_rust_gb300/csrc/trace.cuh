@@ -208,27 +208,43 @@ struct TraceResult {
     float t, b1, b2;
 };
 
-// Closest hit (ANY = false) or any hit (ANY = true).  `status` gets
-// PBRT_ERR_STACK_OVERFLOW (6) if the stack would overflow (the host checks
-// the tree depth first, so this only guards).
-template <int STACK, bool ANY>
-__device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status) {
-    float maxt = r.tmax;
-    bool found = false;
-    res->prim = -1;
-    res->t = 0.0f;
-    res->b1 = 0.0f;
-    res->b2 = 0.0f;
-    if (bvh.empty) return false;
-    float tr;
-    const ChildRec& R = bvh.root;
-    if (!slab(R.lo_x, R.lo_y, R.lo_z, R.hi_x, R.hi_y, R.hi_z, r, maxt, &tr)) return false;
-    uint32_t a = R.a, b = R.b;
+// Per-ray traversal state.  start() tests the root box; step() does one
+// unit of work (one leaf's primitives, or one inner node's two child
+// boxes) and then, if needed, pops the next deferred child; it returns
+// false once the ray is finished.  Closest hit (ANY = false) or any hit
+// (ANY = true, stopping at the first accepted primitive).
+template <int STACK>
+struct Traversal {
+    float maxt;
+    uint32_t a, b;
+    int sp;
+    bool found;
+    TraceResult res;
     uint32_t st_a[STACK];
     uint32_t st_b[STACK];
     float st_t[STACK];
-    int sp = 0;
-    for (;;) {
+
+    __device__ __forceinline__ bool start(const DevBVH& bvh, const DRay& r) {
+        maxt = r.tmax;
+        found = false;
+        sp = 0;
+        res.prim = -1;
+        res.t = 0.0f;
+        res.b1 = 0.0f;
+        res.b2 = 0.0f;
+        if (bvh.empty) return false;
+        float tr;
+        const ChildRec& R = bvh.root;
+        if (!slab(R.lo_x, R.lo_y, R.lo_z, R.hi_x, R.hi_y, R.hi_z, r, maxt, &tr)) return false;
+        a = R.a;
+        b = R.b;
+        return true;
+    }
+
+    // `status` gets PBRT_ERR_STACK_OVERFLOW (6) if the stack would overflow
+    // (the host checks the tree depth first, so this only guards).
+    template <bool ANY>
+    __device__ __forceinline__ bool step(const DevBVH& bvh, const DRay& r, int* status) {
         if (b & kLeafBit) {
             uint32_t cnt = b & kCountMask;
             for (uint32_t i = 0; i < cnt; ++i) {
@@ -247,11 +263,11 @@ __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, Trace
                 if (hit) {
                     maxt = t;
                     found = true;
-                    res->prim = (int32_t)(id & ~kSphereBit);
-                    res->t = t;
-                    res->b1 = b1;
-                    res->b2 = b2;
-                    if (ANY) return true;
+                    res.prim = (int32_t)(id & ~kSphereBit);
+                    res.t = t;
+                    res.b1 = b1;
+                    res.b2 = b2;
+                    if (ANY) return false;
                 }
             }
         } else {
@@ -273,7 +289,7 @@ __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, Trace
                 if (hf) {
                     if (sp == STACK) {
                         *status = 6;
-                        return found;
+                        return false;
                     }
                     st_a[sp] = fa;
                     st_b[sp] = fb;
@@ -282,28 +298,37 @@ __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, Trace
                 }
                 a = na;
                 b = nb;
-                continue;
+                return true;
             }
             if (hf) {
                 a = fa;
                 b = fb;
-                continue;
+                return true;
             }
         }
         // pop the next deferred child whose box still passes
-        bool next = false;
         while (sp > 0) {
             --sp;
             if (!(st_t[sp] > maxt)) {
                 a = st_a[sp];
                 b = st_b[sp];
-                next = true;
-                break;
+                return true;
             }
         }
-        if (!next) break;
+        return false;
     }
-    return found;
+};
+
+// Whole traversal of one ray.
+template <int STACK, bool ANY>
+__device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status) {
+    Traversal<STACK> T;
+    if (T.start(bvh, r)) {
+        while (T.template step<ANY>(bvh, r, status)) {
+        }
+    }
+    *res = T.res;
+    return T.found;
 }
 
 }  // namespace pbrt

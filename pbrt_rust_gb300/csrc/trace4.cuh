@@ -1,0 +1,187 @@
+// trace4.cuh - traversal over the 4-wide layout (layout.h: Node4).
+//
+// Each Node4 holds the four grandchildren of one binary node N of the
+// reference tree.  A visit tests the four child boxes against the current
+// maxt and orders the hits exactly as BVHAccelerator::intersect
+// (src/primitive/aggregates/bvh.rs:390-417) would visit them: N's children
+// in dir_is_neg[axis(N)] order, and inside each, that child's children in
+// dir_is_neg order of its own axis.  The reference also tests the boxes of
+// N's two children; skipping them changes nothing: each is the union of
+// its children's boxes, so its planes are among theirs, and because f32
+// subtraction and multiplication are monotone the child's slab interval
+// always lies inside the parent's - a child that passes implies a parent
+// that passes.  The deferred children are pushed with their entry
+// distance t0 and re-checked against maxt when popped (see trace.cuh), so
+// every box decision, every primitive test and their order are the
+// reference's, and results are bit-identical to it, ties included.
+//
+// The stack lives in shared memory (SMAX 8-byte entries per thread,
+// [entry][thread] so a warp's accesses hit distinct banks) with an
+// optional local-memory overflow of OVF entries; the host picks a variant
+// whose SMAX + OVF covers the tree's bound (HostBVH::stack4_bound).
+#pragma once
+#include <stdint.h>
+
+#include "layout.h"
+#include "trace.cuh"
+
+namespace pbrt {
+
+struct DevBVH4 {
+    const Node4* nodes;
+    const PrimRec* prims;
+    const SphereRec* spheres;
+    ChildRec root;
+    uint32_t empty;
+};
+
+struct ChildV {
+    float lx, ly, lz, hx, hy, hz;
+    uint32_t a, b;
+};
+
+__device__ __forceinline__ ChildV ld_child(const ChildRec* c) {
+    ChildV v;
+    float f0, f1, f2, f3, f4, f5, f6, f7;
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(f0), "=f"(f1), "=f"(f2), "=f"(f3), "=f"(f4), "=f"(f5), "=f"(f6), "=f"(f7)
+                 : "l"(c));
+    v.lx = f0;
+    v.ly = f1;
+    v.lz = f2;
+    v.a = __float_as_uint(f3);
+    v.hx = f4;
+    v.hy = f5;
+    v.hz = f6;
+    v.b = __float_as_uint(f7);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T sel4(uint32_t i, T x0, T x1, T x2, T x3) {
+    return i == 0 ? x0 : (i == 1 ? x1 : (i == 2 ? x2 : x3));
+}
+
+template <int SMAX, int OVF>
+struct Traversal4 {
+    float maxt;
+    uint32_t cur;
+    int sp;
+    bool found;
+    bool overflow;
+    TraceResult res;
+    uint2* sstack;  // this thread's column: entry k at sstack[k * stride]
+    uint32_t stride;
+    uint2 ov[OVF > 0 ? OVF : 1];
+
+    __device__ __forceinline__ void bind(uint2* smem, uint32_t tid, uint32_t nthreads) {
+        sstack = smem + tid;
+        stride = nthreads;
+    }
+
+    __device__ __forceinline__ bool start(const DevBVH4& bvh, const DRay& r) {
+        maxt = r.tmax;
+        found = false;
+        overflow = false;
+        sp = 0;
+        res.prim = -1;
+        res.t = 0.0f;
+        res.b1 = 0.0f;
+        res.b2 = 0.0f;
+        if (bvh.empty) return false;
+        float tr;
+        const ChildRec& R = bvh.root;
+        if (!slab(R.lo_x, R.lo_y, R.lo_z, R.hi_x, R.hi_y, R.hi_z, r, maxt, &tr)) return false;
+        cur = R.a;
+        return true;
+    }
+
+    // The host only launches a variant whose SMAX + OVF covers the tree's
+    // stack bound; a full stack is still caught and reported, never written.
+    __device__ __forceinline__ void push(uint32_t ref, float t0) {
+        if (sp >= SMAX + OVF) {
+            overflow = true;
+            return;
+        }
+        uint2 e = make_uint2(ref, __float_as_uint(t0));
+        if (OVF == 0 || sp < SMAX)
+            sstack[(uint32_t)sp * stride] = e;
+        else
+            ov[sp - SMAX] = e;
+        ++sp;
+    }
+
+    __device__ __forceinline__ bool pop() {
+        while (sp > 0) {
+            --sp;
+            uint2 e = (OVF == 0 || sp < SMAX) ? sstack[(uint32_t)sp * stride] : ov[sp - SMAX];
+            if (!(__uint_as_float(e.y) > maxt)) {
+                cur = e.x;
+                return true;
+            }
+        }
+        return false;
+    }
+
+    template <bool ANY>
+    __device__ __forceinline__ bool step(const DevBVH4& bvh, const DRay& r) {
+        if (cur & kNode4Leaf) {
+            uint32_t off = cur & ~kNode4Leaf;
+            for (;;) {
+                const PrimRec* pr = bvh.prims + off;
+                float4 r0 = ldg4(pr->r0);
+                float4 r1 = ldg4(pr->r1);
+                float4 r2 = ldg4(pr->r2);
+                uint32_t id = __float_as_uint(r0.w);
+                float t, b1 = 0.0f, b2 = 0.0f;
+                bool hit;
+                if (id & kSphereBit)
+                    hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
+                else
+                    hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
+                if (hit) {
+                    maxt = t;
+                    found = true;
+                    res.prim = (int32_t)(id & ~kSphereBit);
+                    res.t = t;
+                    res.b1 = b1;
+                    res.b2 = b2;
+                    if (ANY) return false;
+                }
+                if (__float_as_uint(r2.w) & kPrimLastBit) break;
+                ++off;
+            }
+            return pop();
+        }
+        const Node4* nd = bvh.nodes + cur;
+        ChildV c0 = ld_child(&nd->c[0]), c1 = ld_child(&nd->c[1]);
+        ChildV c2 = ld_child(&nd->c[2]), c3 = ld_child(&nd->c[3]);
+        float t0, t1, t2, t3;
+        bool h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
+        bool h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
+        bool h2 = c2.a != kNode4Empty && slab(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
+        bool h3 = c3.a != kNode4Empty && slab(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+        if (!(h0 | h1 | h2 | h3)) return pop();
+        const uint32_t meta = c0.b;
+        const bool sN = (r.neg >> (meta & 3u)) & 1u;
+        const bool sL = (r.neg >> ((meta >> 2) & 3u)) & 1u;
+        const bool sR = (r.neg >> ((meta >> 4) & 3u)) & 1u;
+        // slot index at each visit position (bvh.rs:409-415 applied at N,
+        // then at the child visited first, then at the other one)
+        const uint32_t la = sL ? 1u : 0u, lb = sL ? 0u : 1u, ra = sR ? 3u : 2u, rb = sR ? 2u : 3u;
+        const uint32_t o0 = sN ? ra : la, o1 = sN ? rb : lb, o2 = sN ? la : ra, o3 = sN ? lb : rb;
+        const bool q0 = sel4(o0, h0, h1, h2, h3), q1 = sel4(o1, h0, h1, h2, h3);
+        const bool q2 = sel4(o2, h0, h1, h2, h3), q3 = sel4(o3, h0, h1, h2, h3);
+        const uint32_t p0 = sel4(o0, c0.a, c1.a, c2.a, c3.a), p1 = sel4(o1, c0.a, c1.a, c2.a, c3.a);
+        const uint32_t p2 = sel4(o2, c0.a, c1.a, c2.a, c3.a), p3 = sel4(o3, c0.a, c1.a, c2.a, c3.a);
+        const float u1 = sel4(o1, t0, t1, t2, t3), u2 = sel4(o2, t0, t1, t2, t3), u3 = sel4(o3, t0, t1, t2, t3);
+        const int first = q0 ? 0 : (q1 ? 1 : (q2 ? 2 : 3));
+        if (q3 && first < 3) push(p3, u3);
+        if (q2 && first < 2) push(p2, u2);
+        if (q1 && first < 1) push(p1, u1);
+        cur = first == 0 ? p0 : (first == 1 ? p1 : (first == 2 ? p2 : p3));
+        return !overflow;
+    }
+};
+
+}  // namespace pbrt

@@ -79,6 +79,18 @@ def assert_hits_match(oracle_bvh, got, want, rays, check_f64=True):
             assert abs(got["t"][i] - t64) <= 1e-5 * abs(t64), (i, got["t"][i], t64)
 
 
+KERNELS = ["plain", "pt", "w4", "w4pt"]
+
+
+@pytest.fixture(params=KERNELS)
+def kernel(request):
+    """Every traversal kernel must give the same, reference-exact results."""
+    prev = abi.get_trace_kernel()
+    abi.set_trace_kernel(request.param, 8)
+    yield request.param
+    abi.set_trace_kernel(*prev)
+
+
 @pytest.fixture(scope="module")
 def soup(oracle):
     prims, rays = G.ray_soup(4096, 1 << 20)
@@ -87,7 +99,7 @@ def soup(oracle):
     return prims, rays, gb, ob
 
 
-def test_ray_soup_closest_hit_matches_oracle(soup):
+def test_ray_soup_closest_hit_matches_oracle(soup, kernel):
     """4096 random triangles, 2^20 rays toward the centre (the plain ray-BVH
     query workload)."""
     prims, rays, gb, ob = soup
@@ -98,12 +110,12 @@ def test_ray_soup_closest_hit_matches_oracle(soup):
     assert_hits_match(ob, got, want, rays)
 
 
-def test_ray_soup_any_hit_matches_oracle(soup):
+def test_ray_soup_any_hit_matches_oracle(soup, kernel):
     prims, rays, gb, ob = soup
     np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
 
 
-def test_host_buffers_match_device_buffers(soup):
+def test_host_buffers_match_device_buffers(soup, kernel):
     """The C ABI stages host buffers (numpy) through the device."""
     prims, rays, gb, ob = soup
     sub = rays[:50000]
@@ -113,7 +125,7 @@ def test_host_buffers_match_device_buffers(soup):
     np.testing.assert_array_equal(gb.intersect_p(sub), dev_any(gb, sub))
 
 
-def test_finite_tmax_and_tmin(soup, oracle):
+def test_finite_tmax_and_tmin(soup, oracle, kernel):
     """Segments (tmin > 0, finite tmax) as shadow rays use them."""
     prims, rays, gb, ob = soup
     r = rays[:200000].copy()
@@ -125,7 +137,7 @@ def test_finite_tmax_and_tmin(soup, oracle):
 
 
 @pytest.mark.parametrize("sm", ["middle", "equal"])
-def test_other_split_methods(oracle, sm):
+def test_other_split_methods(oracle, sm, kernel):
     prims, rays = G.ray_soup(2000, 1 << 16, seed=11)
     gb = GpuBVHAccel(prims, 4, sm)
     ob = oracle.OracleBVH(prims, 4, sm)
@@ -134,7 +146,7 @@ def test_other_split_methods(oracle, sm):
     np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
 
 
-def test_sphere_scene_matches_oracle(oracle):
+def test_sphere_scene_matches_oracle(oracle, kernel):
     """Triangles + 64 translated spheres + the area-light quad; random rays."""
     prims, lights, cam, smp = G.c1_scene(res=64)
     gb = GpuBVHAccel(prims, 4, "sah")
@@ -148,7 +160,7 @@ def test_sphere_scene_matches_oracle(oracle):
     np.testing.assert_array_equal(dev_any(gb, rays), ob.intersect_p(rays))
 
 
-def test_aggregate_kat_on_gpu(oracle):
+def test_aggregate_kat_on_gpu(oracle, kernel):
     """src/primitive/aggregates/mod.rs:93-138 through the device path."""
     from test_kats import get_spheres, ray
     rays = np.concatenate([ray((0, 0, -1), (0, 0, 1)), ray((-1, 0, 2), (1, 0, 0)), ray((4, 0, 0), (-2, 1, 1))])
@@ -158,7 +170,7 @@ def test_aggregate_kat_on_gpu(oracle):
         assert gb.intersect(rays)["prim"].tolist() == [0, 4, 6]
 
 
-def test_tetrahedron_kat_on_gpu():
+def test_tetrahedron_kat_on_gpu(kernel):
     """src/primitive/aggregates/bvh.rs:457-488 through the device path."""
     from test_kats import TET_PTS, TET_TRIS, ray
     mesh = Shape.triangle_mesh(Transform(), None, False, TET_TRIS, TET_PTS)
@@ -169,7 +181,7 @@ def test_tetrahedron_kat_on_gpu():
         assert dev_hits(gb, r)["t"][0] == 1.0
 
 
-def test_partial_sphere_kats_on_gpu():
+def test_partial_sphere_kats_on_gpu(kernel):
     """src/shape/sphere.rs:209-264 as one-sphere aggregates on the device."""
     from test_kats import ray
     xf = Transform.translate((1.0, 2.0, 1.0))
@@ -192,7 +204,7 @@ def test_partial_sphere_kats_on_gpu():
     assert dev_any(s2, ray((0, -4, 10), (0, 0, -1)))[0] == 0
 
 
-def test_edge_cases(oracle):
+def test_edge_cases(oracle, kernel):
     """Empty batches, an empty aggregate, axis-aligned and degenerate rays."""
     torch = _torch()
     from test_kats import TET_PTS, TET_TRIS, ray
