@@ -172,8 +172,9 @@ const char* pbrtgpu_last_error(void);
  * refined, the SAH/middle/equal tree is built on the host with the
  * reference's arithmetic and flattened.
  * An unknown split_method falls back to "sah" with a warning, as
- * bvh.rs:341-349 does.  The device copy is made on the then-current
- * device by the first call that needs it (intersect or render). */
+ * bvh.rs:341-349 does.  When a CUDA device is present the device copy is
+ * made here, on the current device; otherwise the first call that needs
+ * it makes it. */
 int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
                        uint32_t max_prims_in_node, const char* split_method,
                        PbrtBVH** out);
@@ -226,7 +227,8 @@ int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg);
 /* ---- renderer: the GpuSamplerRenderer drop-in ------------------------- */
 
 /* Builds the aggregate plus the device copies of materials and lights
- * (Scene::new_with, src/scene.rs:31-39). */
+ * (Scene::new_with, src/scene.rs:31-39); device residency as for
+ * pbrtgpu_bvh_create. */
 int pbrtgpu_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
 void pbrtgpu_scene_destroy(PbrtScene* scene);
 /* The scene's aggregate, usable with pbrtgpu_intersect*. */

@@ -48,6 +48,15 @@ void DeviceBuf::release() {
     cap = 0;
 }
 
+bool cuda_device_present() {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
 bool is_device_pointer(const void* ptr) {
     if (!ptr) return false;
     cudaPointerAttributes a;
@@ -214,6 +223,12 @@ int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t 
         std::string msg = "BVH depth " + std::to_string(b->host.depth) + " exceeds the deepest traversal stack (256)";
         delete b;
         return set_error(PBRT_ERR_STACK_OVERFLOW, msg);
+    }
+    // Resident from creation when a device is present, so allocation
+    // failures surface here and the first query pays no upload.
+    if (cuda_device_present() && (st = bvh_upload(b))) {
+        delete b;
+        return st;
     }
     *out = b;
     return PBRT_OK;

@@ -16,6 +16,7 @@ namespace pbrt {
 int set_error(int status, const std::string& msg);
 int cuda_status(cudaError_t e, const char* what);
 bool is_device_pointer(const void* p);
+bool cuda_device_present();
 
 // Grow-only device allocation reused across calls.
 struct DeviceBuf {

@@ -293,6 +293,10 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
         }
         S->lights.push_back(r);
     }
+    if (cuda_device_present() && (st = scene_upload(S))) {
+        delete S;
+        return st;
+    }
     *out = S;
     return PBRT_OK;
 }
