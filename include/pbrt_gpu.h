@@ -243,6 +243,25 @@ int pbrtgpu_render(const PbrtScene* scene, const PbrtCameraDesc* camera,
                    const PbrtSamplerDesc* sampler, float* rgb_out,
                    void* stream);
 
+/* pbrtgpu_render without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory while rendering: a serving process that reserves its
+ * memory up front and admits work against that fixed budget, or a frame
+ * loop that cannot afford the device-wide synchronisation cudaMalloc and
+ * cudaFree may cause.  Its scratch is one static array of 64 MiB of device
+ * memory, present on every GPU where the library's code is loaded until the
+ * process exits; a frame needing more (about 220 bytes per sample with two
+ * lights, e.g. 256x256 at 4 spp) is refused with PBRT_ERR_BUDGET, and
+ * num_tasks is limited to 256.  The scene must have its device copy
+ * (pbrtgpu_scene_create makes it when a device is present).  The first call
+ * on a device looks up the scratch's device address; make that first call
+ * before any stream capture.  All calls share the one scratch array: calls
+ * that overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  Results equal pbrtgpu_render's. */
+int pbrtgpu_render_noalloc(const PbrtScene* scene, const PbrtCameraDesc* camera,
+                           const PbrtSamplerDesc* sampler, float* rgb_out,
+                           void* stream);
+
 /* Pixel extent (x0, x1, y0, y1) of the film a camera describes
  * (Film::get_pixel_extent, src/camera/film.rs:301-309). */
 int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* camera, int32_t ext[4]);

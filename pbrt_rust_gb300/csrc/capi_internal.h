@@ -5,11 +5,13 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/pbrt_gpu.h"
 #include "host_scene.h"
 #include "trace.cuh"
 #include "trace4.cuh"
+#include "render_types.h"
 
 namespace pbrt {
 
@@ -55,4 +57,39 @@ struct PbrtBVH {
 namespace pbrt {
 int bvh_upload(PbrtBVH* b);
 const DevBVH4* wide_of(const PbrtBVH* b);
+}
+
+struct PbrtScene {
+    PbrtBVH* bvh = nullptr;
+    std::vector<pbrt::ShadePrim> shade;
+    std::vector<float4> materials;
+    std::vector<pbrt::LightRec> lights;
+    std::vector<pbrt::AreaTri> area_tris;
+    std::vector<float> area_cdf;
+    pbrt::ShadePrim* d_shade = nullptr;
+    float4* d_materials = nullptr;
+    pbrt::LightRec* d_lights = nullptr;
+    pbrt::AreaTri* d_area_tris = nullptr;
+    float* d_area_cdf = nullptr;
+    std::atomic<bool> uploaded{false};
+    std::mutex mu;  // serialises renders: they share the scratch buffers below
+    pbrt::DeviceBuf rays, hits, img, lsamp, contrib, le, L, srays, sslot, occ, counters, tasks, table, rgb;
+    ~PbrtScene() {
+        if (bvh) delete bvh;
+        for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lights, (void*)d_area_tris, (void*)d_area_cdf})
+            if (p) cudaFree(p);
+        for (pbrt::DeviceBuf* b : {&rays, &hits, &img, &lsamp, &contrib, &le, &L, &srays, &sslot, &occ, &counters,
+                                   &tasks, &table, &rgb})
+            b->release();
+    }
+};
+
+namespace pbrt {
+// Render set-up helpers (capi_render.cu), the reference's f32 arithmetic.
+int32_t f2i32(float f);
+size_t f2usize(float f);
+void crop_window(size_t num, size_t count, float aspect, float out[4]);
+void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]);
+void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[4]);
+void chacha_key(uint64_t state, uint32_t key[8]);
 }

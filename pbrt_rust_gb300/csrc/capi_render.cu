@@ -25,31 +25,6 @@ namespace pbrt {
 cudaError_t launch_render(const RenderParams& P, cudaStream_t s);
 }
 
-struct PbrtScene {
-    PbrtBVH* bvh = nullptr;
-    std::vector<ShadePrim> shade;
-    std::vector<float4> materials;
-    std::vector<LightRec> lights;
-    std::vector<AreaTri> area_tris;
-    std::vector<float> area_cdf;
-    ShadePrim* d_shade = nullptr;
-    float4* d_materials = nullptr;
-    LightRec* d_lights = nullptr;
-    AreaTri* d_area_tris = nullptr;
-    float* d_area_cdf = nullptr;
-    std::atomic<bool> uploaded{false};
-    std::mutex mu;  // serialises renders: they share the scratch buffers below
-    DeviceBuf rays, hits, img, lsamp, contrib, le, L, srays, sslot, occ, counters, tasks, table, rgb;
-    ~PbrtScene() {
-        if (bvh) delete bvh;
-        for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lights, (void*)d_area_tris, (void*)d_area_cdf})
-            if (p) cudaFree(p);
-        for (DeviceBuf* b : {&rays, &hits, &img, &lsamp, &contrib, &le, &L, &srays, &sslot, &occ, &counters, &tasks,
-                             &table, &rgb})
-            b->release();
-    }
-};
-
 namespace pbrt {
 
 static float clampf(float x, float lo, float hi) {
@@ -59,20 +34,20 @@ static float clampf(float x, float lo, float hi) {
 }
 
 // Rust `f as i32` / `f as usize` (saturating, NaN -> 0)
-static int32_t f2i32(float f) {
+int32_t f2i32(float f) {
     if (f != f) return 0;
     if (f >= 2147483647.0f) return INT32_MAX;
     if (f <= -2147483648.0f) return INT32_MIN;
     return (int32_t)f;
 }
-static size_t f2usize(float f) {
+size_t f2usize(float f) {
     if (!(f > 0.0f)) return 0;
     if (f >= 18446744073709551615.0f) return SIZE_MAX;
     return (size_t)f;
 }
 
 // src/utils/mod.rs:171-205
-static void crop_window(size_t num, size_t count, float aspect, float out[4]) {
+void crop_window(size_t num, size_t count, float aspect, float out[4]) {
     auto split = [](size_t cnt, size_t asp, size_t* nx, size_t* ny) {
         size_t x = 1, y = cnt;
         while ((y % 2) == 0 && 2 * asp * x < y) {
@@ -98,10 +73,10 @@ static void crop_window(size_t num, size_t count, float aspect, float out[4]) {
     out[3] = (float)(yo + 1) / (float)ny;
 }
 
-static float lerpf(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // utils/mod.rs:15-21
+float lerpf(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // utils/mod.rs:15-21
 
 // src/sampler/base.rs:29-48
-static void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]) {
+void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]) {
     size_t dx = (size_t)(s.x_end - s.x_start), dy = (size_t)(s.y_end - s.y_start);
     float aspect = (float)dx / (float)dy;
     float t[4];
@@ -114,7 +89,7 @@ static void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]) {
 }
 
 // src/camera/film.rs:81-84 -> (x0, x1, y0, y1)
-static void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[4]) {
+void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[4]) {
     int32_t xs = f2i32(std::ceil((float)xres * crop[0]));
     int32_t xc = std::max(f2i32(std::ceil((float)xres * crop[1])) - xs, 1);
     int32_t ys = f2i32(std::ceil((float)yres * crop[2]));
@@ -128,7 +103,7 @@ static void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32
 // rand_core 0.6.4 SeedableRng::seed_from_u64 (the published PCG32 seed
 // expansion: multiplier 6364136223846793005, increment
 // 11634580027462260723, XSH-RR output, state advanced before output).
-static void chacha_key(uint64_t state, uint32_t key[8]) {
+void chacha_key(uint64_t state, uint32_t key[8]) {
     for (int i = 0; i < 8; ++i) {
         state = state * 6364136223846793005ULL + 11634580027462260723ULL;
         uint32_t xs = (uint32_t)(((state >> 18) ^ state) >> 27);
