@@ -210,7 +210,8 @@ int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
  * kernel visits the reference's tree in the reference's order, so results
  * do not depend on the choice.  The first value is also read from the
  * environment (PBRT_TRACE_KERNEL = plain | pt | w4 | w4pt,
- * PBRT_TRACE_REFILL = 1..32) when no call has set it. */
+ * PBRT_TRACE_REFILL = 1..32, PBRT_TRACE_MINB = 0 | 8 | 9,
+ * PBRT_RENDER_KERNEL = plain | w4) when no call has set it. */
 enum {
     PBRT_TRACE_PAIR = 0,            /* binary pairs, one thread per ray */
     PBRT_TRACE_PAIR_PERSISTENT = 1, /* binary pairs, persistent warps */
@@ -218,8 +219,12 @@ enum {
     PBRT_TRACE_WIDE_PERSISTENT = 3  /* 4-wide nodes, persistent warps */
 };
 typedef struct PbrtTraceConfig {
-    int32_t kernel;   /* PBRT_TRACE_* */
-    uint32_t refill;  /* persistent kernels: refill a warp when this many lanes idle */
+    int32_t kernel;         /* PBRT_TRACE_*: pbrtgpu_intersect / intersect_p batches */
+    uint32_t refill;        /* persistent kernels: refill a warp when this many lanes idle */
+    uint32_t min_blocks;    /* 4-wide persistent kernel: 0, or 8 / 9 resident 128-thread
+                               blocks per SM requested (fewer registers per thread) */
+    int32_t render_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and shadow
+                               rays inside pbrtgpu_render (coherent batches) */
 } PbrtTraceConfig;
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg);
 int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg);

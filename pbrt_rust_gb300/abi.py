@@ -92,7 +92,8 @@ class PbrtSamplerDesc(C.Structure):
 
 
 class PbrtTraceConfig(C.Structure):
-    _fields_ = [("kernel", C.c_int32), ("refill", C.c_uint32)]
+    _fields_ = [("kernel", C.c_int32), ("refill", C.c_uint32), ("min_blocks", C.c_uint32),
+                ("render_kernel", C.c_int32)]
 
 
 TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3}
@@ -161,19 +162,35 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     return lib
 
 
-def set_trace_kernel(kernel: str, refill: int = 8) -> None:
-    """Choose the traversal kernel: 'plain', 'pt', 'w4' or 'w4pt'."""
-    lib = load()
-    cfg = PbrtTraceConfig(TRACE_KERNELS[kernel], refill)
-    check(lib.pbrtgpu_set_trace_config(C.byref(cfg)), lib)
-
-
-def get_trace_kernel() -> tuple[str, int]:
+def get_trace_config() -> dict:
     lib = load()
     cfg = PbrtTraceConfig()
     check(lib.pbrtgpu_get_trace_config(C.byref(cfg)), lib)
     names = {v: k for k, v in TRACE_KERNELS.items()}
-    return names[cfg.kernel], cfg.refill
+    return {"kernel": names[cfg.kernel], "refill": cfg.refill, "min_blocks": cfg.min_blocks,
+            "render_kernel": names[cfg.render_kernel]}
+
+
+def set_trace_config(kernel: str | None = None, refill: int | None = None, min_blocks: int | None = None,
+                     render_kernel: str | None = None) -> None:
+    """Choose the traversal kernels ('plain', 'pt', 'w4', 'w4pt'); unset
+    fields keep their current value."""
+    lib = load()
+    cur = get_trace_config()
+    cfg = PbrtTraceConfig(TRACE_KERNELS[kernel or cur["kernel"]], refill or cur["refill"],
+                          cur["min_blocks"] if min_blocks is None else min_blocks,
+                          TRACE_KERNELS[render_kernel or cur["render_kernel"]])
+    check(lib.pbrtgpu_set_trace_config(C.byref(cfg)), lib)
+
+
+def set_trace_kernel(kernel: str, refill: int = 8) -> None:
+    """Choose the kernel of pbrtgpu_intersect / intersect_p batches."""
+    set_trace_config(kernel=kernel, refill=refill)
+
+
+def get_trace_kernel() -> tuple[str, int]:
+    c = get_trace_config()
+    return c["kernel"], c["refill"]
 
 
 def check(status: int, lib: C.CDLL | None = None) -> None:

@@ -293,18 +293,21 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t ca
 }
 
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg) {
-    if (!cfg || set_trace_config(cfg->kernel, cfg->refill))
-        return set_error(PBRT_ERR_INVALID_ARGUMENT, "trace config: kernel must be 0..3 and refill 1..32");
+    if (!cfg || set_trace_config(cfg->kernel, cfg->refill, cfg->min_blocks, cfg->render_kernel))
+        return set_error(PBRT_ERR_INVALID_ARGUMENT,
+                         "trace config: kernel 0..3, refill 1..32, min_blocks 0/8/9, render_kernel 0 or 2");
     return PBRT_OK;
 }
 
 int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg) {
     if (!cfg) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
-    int k;
-    unsigned r;
-    get_trace_config(&k, &r);
+    int k, rk;
+    unsigned r, mb;
+    get_trace_config(&k, &r, &mb, &rk);
     cfg->kernel = k;
     cfg->refill = r;
+    cfg->min_blocks = mb;
+    cfg->render_kernel = rk;
     return PBRT_OK;
 }
 

@@ -485,15 +485,18 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (P.n_samples) {
+        // camera rays of neighbouring pixels are coherent: one thread per
+        // ray keeps them together in a warp
+        const int rk = render_trace_kernel();
         e = launch_trace(P.bvh, P.depth, P.rays, (uint32_t)P.n_samples, reinterpret_cast<PbrtHit*>(P.hits), nullptr,
-                         (int*)&P.counters[2], s, P.has_wide ? &P.bvh4 : nullptr, P.wide_bound);
+                         (int*)&P.counters[2], s, P.has_wide ? &P.bvh4 : nullptr, P.wide_bound, rk);
         if (e != cudaSuccess) return e;
         k_shade<<<blocks_for(P.n_samples, 128), 128, 0, s>>>(P);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         uint64_t max_shadow = P.n_samples * P.n_lights;
         if (max_shadow) {
             const size_t smem = 16 * sizeof(uint2) * 128;
-            int wv = P.has_wide ? wide_stack_variant(P.wide_bound) : 0;
+            int wv = (P.has_wide && rk == 2) ? wide_stack_variant(P.wide_bound) : 0;
             if (wv == 64)
                 k_shadow4<16, 48><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
             else if (wv == 256)

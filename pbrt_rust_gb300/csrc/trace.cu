@@ -105,8 +105,8 @@ __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __res
 
 // 4-wide traversal with persistent warps refilling idle lanes (see
 // k_trace_persistent).
-template <int SMAX, int OVF, bool ANY>
-__global__ void __launch_bounds__(128) k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
+template <int SMAX, int OVF, bool ANY, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
                                                            float4* __restrict__ hits, uint8_t* __restrict__ occ,
                                                            int* __restrict__ status, uint32_t per_warp,
                                                            uint32_t refill) {
@@ -162,20 +162,56 @@ __global__ void __launch_bounds__(128) k_trace4_persistent(DevBVH4 bvh, const fl
 enum { kVariantPairPlain = 0, kVariantPairPersistent = 1, kVariantWidePlain = 2, kVariantWidePersistent = 3 };
 static int g_kernel_variant = -1;
 static unsigned g_refill = 4;
+static unsigned g_min_blocks = 0;
+static int g_render_kernel = kVariantPairPlain;
+
+static int variant_from_name(const char* v, int dflt) {
+    if (!strcmp(v, "plain")) return kVariantPairPlain;
+    if (!strcmp(v, "pt")) return kVariantPairPersistent;
+    if (!strcmp(v, "w4")) return kVariantWidePlain;
+    if (!strcmp(v, "w4pt")) return kVariantWidePersistent;
+    return dflt;
+}
 
 static void read_variant() {
     if (g_kernel_variant >= 0) return;
     g_kernel_variant = kVariantWidePersistent;
-    if (const char* v = getenv("PBRT_TRACE_KERNEL")) {
-        if (!strcmp(v, "plain")) g_kernel_variant = kVariantPairPlain;
-        else if (!strcmp(v, "pt")) g_kernel_variant = kVariantPairPersistent;
-        else if (!strcmp(v, "w4")) g_kernel_variant = kVariantWidePlain;
-        else if (!strcmp(v, "w4pt")) g_kernel_variant = kVariantWidePersistent;
-    }
+    if (const char* v = getenv("PBRT_TRACE_KERNEL")) g_kernel_variant = variant_from_name(v, g_kernel_variant);
     if (const char* r = getenv("PBRT_TRACE_REFILL")) {
         int x = atoi(r);
         if (x >= 1 && x <= 32) g_refill = (unsigned)x;
     }
+    if (const char* m = getenv("PBRT_TRACE_MINB")) {
+        int x = atoi(m);
+        if (x == 0 || x == 8 || x == 9) g_min_blocks = (unsigned)x;
+    }
+    if (const char* v = getenv("PBRT_RENDER_KERNEL")) {
+        int k = variant_from_name(v, g_render_kernel);
+        if (k == kVariantPairPlain || k == kVariantWidePlain) g_render_kernel = k;
+    }
+}
+
+template <int SMAX, int OVF, bool ANY, int MINB>
+static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
+                                          int* d_status, cudaStream_t stream) {
+    const int block = 128;
+    const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
+    static int bps = 0, sms = 0;
+    if (bps == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY, MINB>, block, smem);
+        if (bps < 1) bps = 1;
+    }
+    uint64_t warps = (uint64_t)sms * bps * (block / 32);
+    uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
+    if (per_warp < 32) per_warp = 32;
+    uint64_t need_warps = (n + per_warp - 1) / per_warp;
+    unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
+    k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status,
+                                                                            per_warp, g_refill);
+    return cudaGetLastError();
 }
 
 template <int SMAX, int OVF, bool ANY>
@@ -188,35 +224,32 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
         k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status);
         return cudaGetLastError();
     }
-    static int bps = 0, sms = 0;
-    if (bps == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY>, block, smem);
-        if (bps < 1) bps = 1;
-    }
-    uint64_t warps = (uint64_t)sms * bps * (block / 32);
-    uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
-    if (per_warp < 32) per_warp = 32;
-    uint64_t need_warps = (n + per_warp - 1) / per_warp;
-    unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace4_persistent<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status, per_warp,
-                                                                      g_refill);
-    return cudaGetLastError();
+    if (g_min_blocks == 8) return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, h4, occ, d_status, stream);
+    if (g_min_blocks == 9) return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, h4, occ, d_status, stream);
+    return launch_wide_persistent<SMAX, OVF, ANY, 1>(bvh, r4, n, h4, occ, d_status, stream);
 }
 
-int set_trace_config(int kernel, unsigned refill) {
+int set_trace_config(int kernel, unsigned refill, unsigned min_blocks, int render_kernel) {
     if (kernel < kVariantPairPlain || kernel > kVariantWidePersistent || refill < 1 || refill > 32) return 1;
+    if (!(min_blocks == 0 || min_blocks == 8 || min_blocks == 9)) return 1;
+    if (render_kernel != kVariantPairPlain && render_kernel != kVariantWidePlain) return 1;
     read_variant();
     g_kernel_variant = kernel;
     g_refill = refill;
+    g_min_blocks = min_blocks;
+    g_render_kernel = render_kernel;
     return 0;
 }
-void get_trace_config(int* kernel, unsigned* refill) {
+void get_trace_config(int* kernel, unsigned* refill, unsigned* min_blocks, int* render_kernel) {
     read_variant();
     *kernel = g_kernel_variant;
     *refill = g_refill;
+    *min_blocks = g_min_blocks;
+    *render_kernel = g_render_kernel;
+}
+int render_trace_kernel() {
+    read_variant();
+    return g_render_kernel;
 }
 
 int wide_stack_variant(uint32_t bound) {
@@ -256,13 +289,14 @@ int trace_stack_for_depth(uint32_t depth) {
 
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
-                         uint32_t wide_bound) {
+                         uint32_t wide_bound, int kernel) {
     if (n == 0) return cudaSuccess;
     read_variant();
-    if (wide && (g_kernel_variant == kVariantWidePlain || g_kernel_variant == kVariantWidePersistent)) {
+    const int variant = kernel >= 0 ? kernel : g_kernel_variant;
+    if (wide && (variant == kVariantWidePlain || variant == kVariantWidePersistent)) {
         const float4* r4 = reinterpret_cast<const float4*>(rays);
         float4* h4 = reinterpret_cast<float4*>(hits);
-        const bool any = occluded != nullptr, pt = g_kernel_variant == kVariantWidePersistent;
+        const bool any = occluded != nullptr, pt = variant == kVariantWidePersistent;
         int v = wide_stack_variant(wide_bound);
         if (v == 64)
             return any ? launch_wide<16, 48, true>(*wide, r4, n, nullptr, occluded, d_status, stream, pt)
@@ -277,7 +311,7 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     float4* h4 = reinterpret_cast<float4*>(hits);
     int stack = trace_stack_for_depth(depth);
     bool any = occluded != nullptr;
-    if (g_kernel_variant == kVariantPairPersistent) {
+    if (variant == kVariantPairPersistent) {
         if (stack == 64)
             return any ? launch_persistent<64, true>(bvh, r4, n, nullptr, occluded, d_status, stream)
                        : launch_persistent<64, false>(bvh, r4, n, h4, nullptr, d_status, stream);
