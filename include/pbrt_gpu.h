@@ -248,6 +248,17 @@ int pbrtgpu_render(const PbrtScene* scene, const PbrtCameraDesc* camera,
                    const PbrtSamplerDesc* sampler, float* rgb_out,
                    void* stream);
 
+/* Renders only tasks [task_lo, task_hi) of the sampler's task split
+ * (sampler_renderer.rs:39-75): pixels owned by other tasks come out +0, and
+ * every other pixel equals pbrtgpu_render's, so the sum of the images of
+ * disjoint task ranges covering [0, num_tasks) is pbrtgpu_render's image bit
+ * for bit.  One range per device or process shards a frame with no exchange
+ * but that sum.  No counterpart in the reference: SamplerRenderer::render
+ * (sampler_renderer.rs:146-176) runs all tasks of a frame in one process.
+ * PBRT_ERR_INVALID_ARGUMENT unless task_lo <= task_hi <= num_tasks. */
+int pbrtgpu_render_tasks(const PbrtScene* scene, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler,
+                         uint32_t task_lo, uint32_t task_hi, float* rgb_out, void* stream);
+
 /* pbrtgpu_render without any device allocation.  This entry point has no
  * counterpart in the reference.  It is for callers that cannot allocate
  * device memory while rendering: a serving process that reserves its

@@ -133,6 +133,8 @@ SIGNATURES = {
     "pbrtgpu_scene_destroy": (None, [_P]),
     "pbrtgpu_scene_bvh": (C.c_int, [_P, C.POINTER(_P)]),
     "pbrtgpu_render": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
+    "pbrtgpu_render_tasks": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), C.c_uint32,
+                                       C.c_uint32, _P, _P]),
     "pbrtgpu_render_noalloc": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
     "pbrtgpu_film_pixel_extent": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_int32)]),
 }

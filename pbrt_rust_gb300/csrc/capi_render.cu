@@ -297,9 +297,17 @@ int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* c, int32_t ext[4]) {
 
 int pbrtgpu_render(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp, float* rgb_out,
                    void* stream_v) {
+    if (!smp) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    return pbrtgpu_render_tasks(cS, cam, smp, 0, smp->num_tasks, rgb_out, stream_v);
+}
+
+int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp,
+                         uint32_t task_lo, uint32_t task_hi, float* rgb_out, void* stream_v) {
     PbrtScene* S = const_cast<PbrtScene*>(cS);
     if (!S || !cam || !smp || !rgb_out) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (smp->num_tasks == 0) return set_error(PBRT_ERR_INVALID_ARGUMENT, "num_tasks must be > 0");
+    if (task_lo > task_hi || task_hi > smp->num_tasks)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "task range must satisfy task_lo <= task_hi <= num_tasks");
     if (smp->x_end <= smp->x_start || smp->y_end <= smp->y_start)
         return set_error(PBRT_ERR_INVALID_ARGUMENT, "empty sampler window");
     const uint32_t spp = smp->x_samples * smp->y_samples;
@@ -356,6 +364,7 @@ int pbrtgpu_render(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSam
         sub_window(*smp, t, w);
         chacha_key(t, T.key);
         if (w[0] == w[1] || w[2] == w[3]) continue;  // get_sub_sampler -> None: the task does nothing
+        if (t < task_lo || t >= task_hi) continue;   // another shard's task: owns no pixel here
         T.wx0 = w[0];
         T.wx1 = w[1];
         T.wy0 = w[2];

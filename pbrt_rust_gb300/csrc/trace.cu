@@ -226,7 +226,7 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
     }
     if (g_min_blocks == 8) return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, h4, occ, d_status, stream);
     if (g_min_blocks == 9) return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, h4, occ, d_status, stream);
-    return launch_wide_persistent<SMAX, OVF, ANY, 1>(bvh, r4, n, h4, occ, d_status, stream);
+    return launch_wide_persistent<SMAX, OVF, ANY, 0>(bvh, r4, n, h4, occ, d_status, stream);
 }
 
 int set_trace_config(int kernel, unsigned refill, unsigned min_blocks, int render_kernel) {

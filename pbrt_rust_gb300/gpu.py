@@ -210,9 +210,11 @@ class GpuSamplerRenderer:
         abi.check(self._lib.pbrtgpu_film_pixel_extent(C.byref(self._cam), ext), self._lib)
         return tuple(ext[:])
 
-    def render(self, scene: GpuScene, out=None, stream=None):
+    def render(self, scene: GpuScene, out=None, stream=None, tasks: tuple[int, int] | None = None):
         """Renderer::render: returns (h, w, 3) float32 linear RGB (a numpy
-        array, or `out` if given: a host array or a CUDA tensor)."""
+        array, or `out` if given: a host array or a CUDA tensor).  With
+        ``tasks=(lo, hi)`` only those tasks of the split are rendered and the
+        pixels of the others are 0 (one shard of a frame)."""
         x0, x1, y0, y1 = self.pixel_extent()
         shape = (y1 - y0, x1 - x0, 3)
         if out is None:
@@ -223,6 +225,11 @@ class GpuSamplerRenderer:
             if out.shape != shape or out.dtype != np.float32 or not out.flags.c_contiguous:
                 raise ValueError(f"out must be a contiguous float32 array of shape {shape}")
             ptr = C.c_void_p(out.ctypes.data)
-        abi.check(self._lib.pbrtgpu_render(scene._h, C.byref(self._cam), C.byref(self._smp), ptr,
-                                           _stream_handle(stream)), self._lib)
+        if tasks is None:
+            st = self._lib.pbrtgpu_render(scene._h, C.byref(self._cam), C.byref(self._smp), ptr,
+                                          _stream_handle(stream))
+        else:
+            st = self._lib.pbrtgpu_render_tasks(scene._h, C.byref(self._cam), C.byref(self._smp), int(tasks[0]),
+                                                int(tasks[1]), ptr, _stream_handle(stream))
+        abi.check(st, self._lib)
         return out

@@ -96,3 +96,16 @@ def test_no_cpu_fallback_without_a_gpu(lib):
     with pytest.raises(abi.PbrtError) as e:
         g.intersect(rays)
     assert e.value.status in (2, 10)
+
+
+def test_render_task_range_is_checked(lib):
+    """pbrtgpu_render_tasks rejects a range outside [0, num_tasks] before any
+    device work."""
+    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
+    prims, lights, cam, smp = G.c1_scene(res=16, n_spheres=2)
+    scene = GpuScene(prims, lights)
+    r = GpuSamplerRenderer(smp, cam, num_tasks=4)
+    for lo, hi in ((3, 2), (0, 5)):
+        with pytest.raises(abi.PbrtError) as e:
+            r.render(scene, tasks=(lo, hi))
+        assert e.value.status == 1 and b"task range" in lib.pbrtgpu_last_error()
