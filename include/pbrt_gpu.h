@@ -211,7 +211,8 @@ int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
  * do not depend on the choice.  The first value is also read from the
  * environment (PBRT_TRACE_KERNEL = plain | pt | w4 | w4pt,
  * PBRT_TRACE_REFILL = 1..32, PBRT_TRACE_MINB = 0 | 8 | 9,
- * PBRT_RENDER_KERNEL = plain | w4) when no call has set it. */
+ * PBRT_RENDER_KERNEL = plain | w4, PBRT_TRACE_REORDER = 0 | 1,
+ * PBRT_TRACE_CHUNK = 0 | 32..4096) when no call has set it. */
 enum {
     PBRT_TRACE_PAIR = 0,            /* binary pairs, one thread per ray */
     PBRT_TRACE_PAIR_PERSISTENT = 1, /* binary pairs, persistent warps */
@@ -225,6 +226,12 @@ typedef struct PbrtTraceConfig {
                                blocks per SM requested (fewer registers per thread) */
     int32_t render_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and shadow
                                rays inside pbrtgpu_render (coherent batches) */
+    uint32_t reorder;       /* 1: pbrtgpu_intersect / intersect_p batches of 32768 rays
+                               or more are binned by direction and origin before
+                               traversal (same results, more coherent warps) */
+    uint32_t chunk;         /* 4-wide persistent kernel: 0 = each warp owns a fixed
+                               range of the batch; 32..4096 (a multiple of 32) = warps
+                               take this many rays at a time from a shared counter */
 } PbrtTraceConfig;
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg);
 int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg);

@@ -93,7 +93,7 @@ class PbrtSamplerDesc(C.Structure):
 
 class PbrtTraceConfig(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("refill", C.c_uint32), ("min_blocks", C.c_uint32),
-                ("render_kernel", C.c_int32)]
+                ("render_kernel", C.c_int32), ("reorder", C.c_uint32), ("chunk", C.c_uint32)]
 
 
 TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3}
@@ -170,18 +170,21 @@ def get_trace_config() -> dict:
     check(lib.pbrtgpu_get_trace_config(C.byref(cfg)), lib)
     names = {v: k for k, v in TRACE_KERNELS.items()}
     return {"kernel": names[cfg.kernel], "refill": cfg.refill, "min_blocks": cfg.min_blocks,
-            "render_kernel": names[cfg.render_kernel]}
+            "render_kernel": names[cfg.render_kernel], "reorder": bool(cfg.reorder), "chunk": cfg.chunk}
 
 
 def set_trace_config(kernel: str | None = None, refill: int | None = None, min_blocks: int | None = None,
-                     render_kernel: str | None = None) -> None:
-    """Choose the traversal kernels ('plain', 'pt', 'w4', 'w4pt'); unset
-    fields keep their current value."""
+                     render_kernel: str | None = None, reorder: bool | None = None,
+                     chunk: int | None = None) -> None:
+    """Choose the traversal kernels ('plain', 'pt', 'w4', 'w4pt') and their
+    options; unset fields keep their current value."""
     lib = load()
     cur = get_trace_config()
     cfg = PbrtTraceConfig(TRACE_KERNELS[kernel or cur["kernel"]], refill or cur["refill"],
                           cur["min_blocks"] if min_blocks is None else min_blocks,
-                          TRACE_KERNELS[render_kernel or cur["render_kernel"]])
+                          TRACE_KERNELS[render_kernel or cur["render_kernel"]],
+                          int(cur["reorder"] if reorder is None else reorder),
+                          cur["chunk"] if chunk is None else chunk)
     check(lib.pbrtgpu_set_trace_config(C.byref(cfg)), lib)
 
 

@@ -1,6 +1,7 @@
 // capi.cu - the C ABI declared in include/pbrt_gpu.h.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -120,6 +121,86 @@ const DevBVH4* wide_of(const PbrtBVH* b) {
     return wide_stack_variant(b->host.stack4_bound) ? &b->dev4 : nullptr;
 }
 
+// Stream-ordered scratch for per-call temporaries (the ray permutation):
+// one pool per device owned by the library, which keeps freed memory for the
+// next call instead of returning it to the driver at every synchronisation.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[16];
+
+static int scratch_pool(int dev, cudaMemPool_t* out) {
+    if (dev < 0 || dev >= 16) return set_error(PBRT_ERR_UNSUPPORTED, "device index above 15");
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        int st = cuda_status(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate");
+        if (st) return st;
+        uint64_t keep = ~0ull;
+        if ((st = cuda_status(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep),
+                              "cudaMemPoolSetAttribute"))) {
+            cudaMemPoolDestroy(pool);
+            return st;
+        }
+        g_pools[dev] = pool;
+    }
+    *out = g_pools[dev];
+    return PBRT_OK;
+}
+
+// Traces device-resident rays, first binning a large batch by direction and
+// origin when the configuration asks for it (reorder.cu); the permutation
+// lives in stream-ordered scratch released on the same stream.
+static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* d_hits, uint8_t* d_occ,
+                        cudaStream_t s) {
+    const uint32_t* order = nullptr;
+    uint32_t* work = nullptr;
+    void* scratch = nullptr;
+    int st;
+    const bool reorder = trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
+    const bool chunked = trace_chunk() != 0;
+    if (reorder || chunked) {
+        // [256 B: chunk counter][permutation scratch]
+        cudaMemPool_t pool;
+        if ((st = scratch_pool(b->device, &pool))) return st;
+        const size_t bytes = 256 + (reorder ? ray_order_scratch_bytes(n) : 0);
+        if ((st = cuda_status(cudaMallocFromPoolAsync(&scratch, bytes, pool, s), "cudaMallocFromPoolAsync")))
+            return st;
+        work = static_cast<uint32_t*>(scratch);
+        if ((st = cuda_status(cudaMemsetAsync(work, 0, sizeof(uint32_t), s), "cudaMemsetAsync"))) {
+            cudaFreeAsync(scratch, s);
+            return st;
+        }
+        if (!chunked) work = nullptr;
+    }
+    if (reorder) {
+        const Box& wb = b->host.nodes[0].box;
+        ReorderBounds B;
+        const float lo[3] = {wb.lo.x, wb.lo.y, wb.lo.z}, hi[3] = {wb.hi.x, wb.hi.y, wb.hi.z};
+        const float cells[3] = {8.0f, 4.0f, 4.0f};
+        for (int k = 0; k < 3; ++k) {
+            float ext = hi[k] - lo[k];
+            B.lo[k] = std::isfinite(lo[k]) ? lo[k] : 0.0f;
+            B.scale[k] = (ext > 0.0f && std::isfinite(ext)) ? cells[k] / ext : 0.0f;
+        }
+        uint32_t* ord = nullptr;
+        if ((st = cuda_status(build_ray_order(d_rays, n, B, static_cast<unsigned char*>(scratch) + 256, &ord, s),
+                              "ray reorder"))) {
+            cudaFreeAsync(scratch, s);
+            return st;
+        }
+        order = ord;
+    }
+    st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, d_hits, d_occ, b->d_status, s, wide_of(b),
+                                  b->host.stack4_bound, -1, order, work),
+                     "trace launch");
+    if (scratch) cudaFreeAsync(scratch, s);
+    return st;
+}
+
 // Runs closest/any hit for host or device buffers.
 static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHit* hits, uint8_t* occ,
                       void* stream_v) {
@@ -134,10 +215,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
     void* out = hits ? (void*)hits : (void*)occ;
     size_t out_bytes = hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n;
     bool dr = is_device_pointer(rays), dout = is_device_pointer(out);
-    if (dr && dout)
-        return cuda_status(launch_trace(b->dev, b->host.depth, rays, n, hits, occ, b->d_status, s, wide_of(b),
-                                        b->host.stack4_bound),
-                           "trace launch");
+    if (dr && dout) return launch_batch(b, rays, n, hits, occ, s);
     std::lock_guard<std::mutex> lk(b->stage_mu);
     const PbrtRay* d_rays = rays;
     if (!dr) {
@@ -153,10 +231,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
         if ((st = b->stage_out.reserve(out_bytes))) return st;
         d_out = b->stage_out.p;
     }
-    if ((st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, hits ? (PbrtHit*)d_out : nullptr,
-                                       hits ? nullptr : (uint8_t*)d_out, b->d_status, s, wide_of(b),
-                                       b->host.stack4_bound),
-                          "trace launch")))
+    if ((st = launch_batch(b, d_rays, n, hits ? (PbrtHit*)d_out : nullptr, hits ? nullptr : (uint8_t*)d_out, s)))
         return st;
     if (!dout &&
         (st = cuda_status(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H")))
@@ -293,21 +368,16 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t ca
 }
 
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg) {
-    if (!cfg || set_trace_config(cfg->kernel, cfg->refill, cfg->min_blocks, cfg->render_kernel))
+    if (!cfg || set_trace_config(*cfg))
         return set_error(PBRT_ERR_INVALID_ARGUMENT,
-                         "trace config: kernel 0..3, refill 1..32, min_blocks 0/8/9, render_kernel 0 or 2");
+                         "trace config: kernel 0..3, refill 1..32, min_blocks 0/8/9, render_kernel 0 or 2, "
+                         "reorder 0/1");
     return PBRT_OK;
 }
 
 int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg) {
     if (!cfg) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
-    int k, rk;
-    unsigned r, mb;
-    get_trace_config(&k, &r, &mb, &rk);
-    cfg->kernel = k;
-    cfg->refill = r;
-    cfg->min_blocks = mb;
-    cfg->render_kernel = rk;
+    get_trace_config(cfg);
     return PBRT_OK;
 }
 

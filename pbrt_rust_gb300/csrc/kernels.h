@@ -17,13 +17,38 @@ int trace_stack_for_depth(uint32_t depth);
 // All pointers are device pointers; d_status receives a PbrtStatus > 0 on a
 // device-side failure.
 // `wide` (may be null) selects the 4-wide layout with the given stack bound.
-// `kernel` >= 0 overrides the process-wide choice (PBRT_TRACE_*).
+// `kernel` >= 0 overrides the process-wide choice (PBRT_TRACE_*).  With
+// `order` (a permutation of [0, n)) the kernels take ray order[j] as their
+// j-th ray; hits still land at each ray's own index.  `work` is the 4-wide
+// persistent kernel's chunk counter (see trace_chunk).
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide = nullptr,
-                         uint32_t wide_bound = 0, int kernel = -1);
-// Process-wide traversal kernel choice (PBRT_TRACE_*); 0 on success.
-int set_trace_config(int kernel, unsigned refill, unsigned min_blocks, int render_kernel);
-void get_trace_config(int* kernel, unsigned* refill, unsigned* min_blocks, int* render_kernel);
+                         uint32_t wide_bound = 0, int kernel = -1, const uint32_t* order = nullptr,
+                         uint32_t* work = nullptr);
+// Process-wide traversal configuration (PBRT_TRACE_* and the environment
+// variables of pbrt_gpu.h); set returns 0 on success, 1 for invalid fields.
+int set_trace_config(const PbrtTraceConfig& cfg);
+void get_trace_config(PbrtTraceConfig* cfg);
+// Batches of at least this many rays are reordered when the configuration
+// asks for it (smaller ones gain nothing from it).
+constexpr uint32_t kReorderMinRays = 1u << 15;
+bool trace_reorder();
+// Rays a warp of the 4-wide persistent kernel takes from a shared counter at
+// a time (0: fixed per-warp ranges).  The counter (`work` of launch_trace,
+// 4 bytes, zero at launch) is the caller's.
+unsigned trace_chunk();
+
+// Coherence ordering of a ray batch (reorder.cu).  `scale` maps an origin
+// inside the world bounds to [0, 8) x [0, 4) x [0, 4).
+struct ReorderBounds {
+    float lo[3];
+    float scale[3];
+};
+size_t ray_order_scratch_bytes(uint32_t n);
+// Fills the permutation at the start of `scratch` (ray_order_scratch_bytes(n)
+// bytes, 256-byte aligned) and returns it in *order; stream-ordered.
+cudaError_t build_ray_order(const PbrtRay* rays, uint32_t n, const ReorderBounds& bounds, void* scratch,
+                            uint32_t** order, cudaStream_t stream);
 // Kernel used for the coherent camera and shadow rays of a render.
 int render_trace_kernel();
 // 64 or 256 when a compiled 4-wide variant covers this stack bound, else 0.

@@ -15,10 +15,12 @@ namespace pbrt {
 // closest hit is one 16-byte store, an any-hit answer one byte.
 template <int STACK, bool ANY>
 __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
-                                               float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                               const uint32_t* __restrict__ order, float4* __restrict__ hits,
+    uint8_t* __restrict__ occ,
                                                int* __restrict__ status) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order) i = __ldg(order + i);
     float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
     DRay r = make_dray(a, b);
     TraceResult res;
@@ -39,7 +41,8 @@ __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restr
 // are identical to k_trace.
 template <int STACK, bool ANY>
 __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
-                                                          float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                          const uint32_t* __restrict__ order, float4* __restrict__ hits,
+    uint8_t* __restrict__ occ,
                                                           int* __restrict__ status, uint32_t per_warp,
                                                           uint32_t refill) {
     const unsigned lane = threadIdx.x & 31u;
@@ -65,8 +68,8 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
             if (ray == kNone) {
                 uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
                 if (my < end) {
-                    ray = (uint32_t)my;
-                    r = make_dray(__ldg(rays + 2 * my), __ldg(rays + 2 * my + 1));
+                    ray = order ? __ldg(order + my) : (uint32_t)my;
+                    r = make_dray(__ldg(rays + 2 * (size_t)ray), __ldg(rays + 2 * (size_t)ray + 1));
                     if (!T.start(bvh, r)) finish();
                 }
             }
@@ -85,11 +88,13 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
 // 4-wide traversal, one thread per ray.
 template <int SMAX, int OVF, bool ANY>
 __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
-                                                float4* __restrict__ hits, uint8_t* __restrict__ occ,
+                                                const uint32_t* __restrict__ order, float4* __restrict__ hits,
+    uint8_t* __restrict__ occ,
                                                 int* __restrict__ status) {
     extern __shared__ uint2 smem_stack[];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (order) i = __ldg(order + i);
     DRay r = make_dray(__ldg(rays + 2 * (size_t)i), __ldg(rays + 2 * (size_t)i + 1));
     Traversal4<SMAX, OVF> T;
     T.bind(smem_stack, threadIdx.x, blockDim.x);
@@ -104,17 +109,22 @@ __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __res
 }
 
 // 4-wide traversal with persistent warps refilling idle lanes (see
-// k_trace_persistent).
+// k_trace_persistent).  Without `work`, warp w owns rays
+// [w * per_warp, (w + 1) * per_warp); with it, warps take chunks of
+// per_warp rays from the shared counter *work (zero at launch) whenever
+// their chunk is used up, so warps that drew short rays take more of them
+// and no warp is left with a long tail.
 template <int SMAX, int OVF, bool ANY, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
-                                                           float4* __restrict__ hits, uint8_t* __restrict__ occ,
-                                                           int* __restrict__ status, uint32_t per_warp,
-                                                           uint32_t refill) {
+__global__ void __launch_bounds__(128, MINB)
+    k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ order,
+                        float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status,
+                        uint32_t per_warp, uint32_t refill, uint32_t* __restrict__ work) {
     extern __shared__ uint2 smem_stack[];
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint64_t next = warp * per_warp;
-    const uint64_t end = (next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n;
+    uint64_t next = work ? 0 : warp * per_warp;
+    uint64_t end = work ? 0 : ((next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n);
+    bool more = work != nullptr;  // the shared counter may still hold rays
     const uint32_t kNone = 0xffffffffu;
     uint32_t ray = kNone;
     bool overflow = false;
@@ -124,12 +134,24 @@ __global__ void __launch_bounds__(128, MINB) k_trace4_persistent(DevBVH4 bvh, co
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
         unsigned nidle = __popc(idle);
-        if (next < end && nidle >= (next + nidle >= end ? 1u : refill)) {
+        if (more && next >= end && nidle >= refill) {  // warp-uniform
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, per_warp);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base < n) {
+                next = base;
+                end = (uint64_t)base + per_warp < (uint64_t)n ? (uint64_t)base + per_warp : (uint64_t)n;
+            } else {
+                more = false;
+            }
+        }
+        const bool tail = !more && next + nidle >= end;
+        if (next < end && nidle >= (tail ? 1u : refill)) {
             if (ray == kNone) {
                 uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
                 if (my < end) {
-                    ray = (uint32_t)my;
-                    r = make_dray(__ldg(rays + 2 * my), __ldg(rays + 2 * my + 1));
+                    ray = order ? __ldg(order + my) : (uint32_t)my;
+                    r = make_dray(__ldg(rays + 2 * (size_t)ray), __ldg(rays + 2 * (size_t)ray + 1));
                     bool live = T.start(bvh, r);
                     if (!live) {
                         if (ANY)
@@ -144,7 +166,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace4_persistent(DevBVH4 bvh, co
         }
         bool busy = ray != kNone;
         if (!__any_sync(0xffffffffu, busy)) {
-            if (next >= end) break;
+            if (next >= end && !more) break;
             continue;
         }
         if (busy && !T.template step<ANY>(bvh, r)) {
@@ -164,6 +186,8 @@ static int g_kernel_variant = -1;
 static unsigned g_refill = 4;
 static unsigned g_min_blocks = 0;
 static int g_render_kernel = kVariantPairPlain;
+static unsigned g_reorder = 0;
+static unsigned g_chunk = 64;
 
 static int variant_from_name(const char* v, int dflt) {
     if (!strcmp(v, "plain")) return kVariantPairPlain;
@@ -185,6 +209,13 @@ static void read_variant() {
         int x = atoi(m);
         if (x == 0 || x == 8 || x == 9) g_min_blocks = (unsigned)x;
     }
+    if (const char* v = getenv("PBRT_TRACE_CHUNK")) {
+        int x = atoi(v);
+        if (x == 0 || (x >= 32 && x <= 4096 && x % 32 == 0)) g_chunk = (unsigned)x;
+    }
+    if (const char* v = getenv("PBRT_TRACE_REORDER")) {
+        if (!strcmp(v, "0") || !strcmp(v, "1")) g_reorder = (unsigned)(v[0] - '0');
+    }
     if (const char* v = getenv("PBRT_RENDER_KERNEL")) {
         int k = variant_from_name(v, g_render_kernel);
         if (k == kVariantPairPlain || k == kVariantWidePlain) g_render_kernel = k;
@@ -192,8 +223,9 @@ static void read_variant() {
 }
 
 template <int SMAX, int OVF, bool ANY, int MINB>
-static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
-                                          int* d_status, cudaStream_t stream) {
+static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
+                                          float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
+                                          uint32_t* work) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
     static int bps = 0, sms = 0;
@@ -207,45 +239,71 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
     uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
     if (per_warp < 32) per_warp = 32;
+    if (work && g_chunk && n <= 0xF0000000u) {  // the counter cannot wrap past n
+        // every resident warp, each taking g_chunk rays at a time; no more
+        // warps than chunks
+        uint64_t chunks = (n + g_chunk - 1) / g_chunk;
+        uint64_t w = chunks < warps ? chunks : warps;
+        unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
+        k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ,
+                                                                                d_status, g_chunk, g_refill, work);
+        return cudaGetLastError();
+    }
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status,
-                                                                            per_warp, g_refill);
+    k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status,
+                                                                            per_warp, g_refill, nullptr);
     return cudaGetLastError();
 }
 
 template <int SMAX, int OVF, bool ANY>
-static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
-                               int* d_status, cudaStream_t stream, bool persistent) {
+static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order, float4* h4,
+                               uint8_t* occ, int* d_status, cudaStream_t stream, bool persistent, uint32_t* work) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
     if (!persistent) {
         unsigned grid = (unsigned)((n + block - 1) / block);
-        k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, h4, occ, d_status);
+        k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status);
         return cudaGetLastError();
     }
-    if (g_min_blocks == 8) return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, h4, occ, d_status, stream);
-    if (g_min_blocks == 9) return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, h4, occ, d_status, stream);
-    return launch_wide_persistent<SMAX, OVF, ANY, 0>(bvh, r4, n, h4, occ, d_status, stream);
+    if (g_min_blocks == 8)
+        return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, order, h4, occ, d_status, stream, work);
+    if (g_min_blocks == 9)
+        return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, order, h4, occ, d_status, stream, work);
+    return launch_wide_persistent<SMAX, OVF, ANY, 0>(bvh, r4, n, order, h4, occ, d_status, stream, work);
 }
 
-int set_trace_config(int kernel, unsigned refill, unsigned min_blocks, int render_kernel) {
-    if (kernel < kVariantPairPlain || kernel > kVariantWidePersistent || refill < 1 || refill > 32) return 1;
-    if (!(min_blocks == 0 || min_blocks == 8 || min_blocks == 9)) return 1;
-    if (render_kernel != kVariantPairPlain && render_kernel != kVariantWidePlain) return 1;
+int set_trace_config(const PbrtTraceConfig& c) {
+    if (c.kernel < kVariantPairPlain || c.kernel > kVariantWidePersistent || c.refill < 1 || c.refill > 32) return 1;
+    if (!(c.min_blocks == 0 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
+    if (c.render_kernel != kVariantPairPlain && c.render_kernel != kVariantWidePlain) return 1;
+    if (c.reorder > 1) return 1;
+    if (!(c.chunk == 0 || (c.chunk >= 32 && c.chunk <= 4096 && c.chunk % 32 == 0))) return 1;
     read_variant();
-    g_kernel_variant = kernel;
-    g_refill = refill;
-    g_min_blocks = min_blocks;
-    g_render_kernel = render_kernel;
+    g_kernel_variant = c.kernel;
+    g_refill = c.refill;
+    g_min_blocks = c.min_blocks;
+    g_render_kernel = c.render_kernel;
+    g_reorder = c.reorder;
+    g_chunk = c.chunk;
     return 0;
 }
-void get_trace_config(int* kernel, unsigned* refill, unsigned* min_blocks, int* render_kernel) {
+void get_trace_config(PbrtTraceConfig* c) {
     read_variant();
-    *kernel = g_kernel_variant;
-    *refill = g_refill;
-    *min_blocks = g_min_blocks;
-    *render_kernel = g_render_kernel;
+    c->kernel = g_kernel_variant;
+    c->refill = g_refill;
+    c->min_blocks = g_min_blocks;
+    c->render_kernel = g_render_kernel;
+    c->reorder = g_reorder;
+    c->chunk = g_chunk;
+}
+unsigned trace_chunk() {
+    read_variant();
+    return g_chunk;
+}
+bool trace_reorder() {
+    read_variant();
+    return g_reorder != 0;
 }
 int render_trace_kernel() {
     read_variant();
@@ -259,8 +317,8 @@ int wide_stack_variant(uint32_t bound) {
 }
 
 template <int STACK, bool ANY>
-static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, float4* h4, uint8_t* occ,
-                                     int* d_status, cudaStream_t stream) {
+static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, const uint32_t* order,
+                                     float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream) {
     static int blocks_per_sm[2][2] = {{0, 0}, {0, 0}};
     static int sms = 0;
     const int block = 128;
@@ -277,7 +335,8 @@ static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32
     if (per_warp < 32) per_warp = 32;
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace_persistent<STACK, ANY><<<grid, block, 0, stream>>>(bvh, r4, n, h4, occ, d_status, per_warp, g_refill);
+    k_trace_persistent<STACK, ANY><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, occ, d_status, per_warp,
+                                                               g_refill);
     return cudaGetLastError();
 }
 
@@ -289,7 +348,7 @@ int trace_stack_for_depth(uint32_t depth) {
 
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
-                         uint32_t wide_bound, int kernel) {
+                         uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work) {
     if (n == 0) return cudaSuccess;
     read_variant();
     const int variant = kernel >= 0 ? kernel : g_kernel_variant;
@@ -299,11 +358,11 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
         const bool any = occluded != nullptr, pt = variant == kVariantWidePersistent;
         int v = wide_stack_variant(wide_bound);
         if (v == 64)
-            return any ? launch_wide<16, 48, true>(*wide, r4, n, nullptr, occluded, d_status, stream, pt)
-                       : launch_wide<16, 48, false>(*wide, r4, n, h4, nullptr, d_status, stream, pt);
+            return any ? launch_wide<16, 48, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work)
+                       : launch_wide<16, 48, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work);
         if (v == 256)
-            return any ? launch_wide<16, 240, true>(*wide, r4, n, nullptr, occluded, d_status, stream, pt)
-                       : launch_wide<16, 240, false>(*wide, r4, n, h4, nullptr, d_status, stream, pt);
+            return any ? launch_wide<16, 240, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work)
+                       : launch_wide<16, 240, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work);
     }
     const int block = 128;
     const unsigned grid = (unsigned)((n + block - 1) / block);
@@ -313,23 +372,23 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     bool any = occluded != nullptr;
     if (variant == kVariantPairPersistent) {
         if (stack == 64)
-            return any ? launch_persistent<64, true>(bvh, r4, n, nullptr, occluded, d_status, stream)
-                       : launch_persistent<64, false>(bvh, r4, n, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<64, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
+                       : launch_persistent<64, false>(bvh, r4, n, order, h4, nullptr, d_status, stream);
         if (stack == 256)
-            return any ? launch_persistent<256, true>(bvh, r4, n, nullptr, occluded, d_status, stream)
-                       : launch_persistent<256, false>(bvh, r4, n, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<256, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
+                       : launch_persistent<256, false>(bvh, r4, n, order, h4, nullptr, d_status, stream);
         return cudaErrorInvalidValue;
     }
     if (stack == 64) {
         if (any)
-            k_trace<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, nullptr, occluded, d_status);
+            k_trace<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status);
         else
-            k_trace<64, false><<<grid, block, 0, stream>>>(bvh, r4, n, h4, nullptr, d_status);
+            k_trace<64, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status);
     } else if (stack == 256) {
         if (any)
-            k_trace<256, true><<<grid, block, 0, stream>>>(bvh, r4, n, nullptr, occluded, d_status);
+            k_trace<256, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status);
         else
-            k_trace<256, false><<<grid, block, 0, stream>>>(bvh, r4, n, h4, nullptr, d_status);
+            k_trace<256, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status);
     } else {
         return cudaErrorInvalidValue;
     }

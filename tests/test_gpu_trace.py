@@ -235,3 +235,32 @@ def test_world_bound_matches_oracle(soup):
     prims, rays, gb, ob = soup
     for a, b in zip(gb.world_bound(), ob.world_bound()):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name,reorder,chunk", [("plain", True, 0), ("pt", True, 0), ("w4", True, 0),
+                                                ("w4pt", True, 0), ("w4pt", True, 64), ("w4pt", False, 32),
+                                                ("w4pt", False, 256)])
+def test_reordered_batches_are_bit_identical(oracle, name, reorder, chunk):
+    """With ray reordering on, batches of 32768+ rays are binned by direction
+    and origin before traversal; with a chunk size, the persistent warps take
+    rays from a shared counter.  Every hit must still equal the oracle's, at
+    its own index, for host and device buffers."""
+    before = abi.get_trace_config()
+    abi.set_trace_config(kernel=name, reorder=reorder, chunk=chunk)
+    try:
+        prims, _ = G.ray_soup(4096, 1, seed=9)
+        lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+        rays = G.incoherent_rays(G.PCG32(77), 1 << 17, lo, hi)
+        g = GpuBVHAccel(prims, 4, "sah")
+        o = oracle.OracleBVH(prims, 4, "sah")
+        want = o.intersect(rays)
+        assert (want["prim"] >= 0).sum() > 1000
+        for got in (g.intersect(rays), dev_hits(g, rays)):
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        want_any = o.intersect_p(rays)
+        assert np.array_equal(g.intersect_p(rays), want_any)
+        assert np.array_equal(dev_any(g, rays), want_any)
+        small = rays[:1000]  # below the reorder threshold
+        assert np.array_equal(g.intersect(small).view(np.uint32), want[:1000].view(np.uint32))
+    finally:
+        abi.set_trace_config(**before)
