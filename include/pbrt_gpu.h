@@ -285,6 +285,85 @@ int pbrtgpu_render_noalloc(const PbrtScene* scene, const PbrtCameraDesc* camera,
                            const PbrtSamplerDesc* sampler, float* rgb_out,
                            void* stream);
 
+/* ---- batched multi-scene wavefront -----------------------------------
+ * No counterpart in the reference: SamplerRenderer::render
+ * (sampler_renderer.rs:146-176) renders one scene per call and
+ * BVHAccelerator::intersect (bvh.rs:375-422) answers one ray per call.  A
+ * batch collects many render jobs (what pbrtgpu_render takes) and ray-query
+ * jobs (what pbrtgpu_intersect / intersect_p take) over any number of
+ * scenes and runs them together: each stage of the wavefront is one launch
+ * over the items of every job, the traversal stages are persistent kernels
+ * fed by a device work counter, and the launch sequence is replayed as one
+ * CUDA graph.  Every job's output equals what the single-job entry point
+ * gives for it (bit for bit).
+ *
+ * Life cycle: create (all device and pinned memory is allocated here, sized
+ * by the limits; pbrtgpu_batch_bytes tells the device bytes up front) ->
+ * add jobs -> launch (asynchronous on the stream) -> wait (copies host
+ * outputs, reports per-job status, empties the batch) -> add ... A job that
+ * would exceed a limit is refused with PBRT_ERR_BUDGET and the batch stays
+ * as it was.  Scenes, BVHs and output buffers must stay valid until wait
+ * returns.  One batch is used by one host thread at a time. */
+typedef struct PbrtBatchLimits {
+    uint32_t max_jobs;          /* render + query jobs per launch */
+    uint32_t max_tasks;         /* render tasks over all render jobs */
+    uint64_t max_samples;       /* camera samples over all render jobs */
+    uint64_t max_light_samples; /* camera samples x lights over all render jobs */
+    uint64_t max_film_pixels;   /* film pixels over all render jobs */
+    uint64_t max_query_rays;    /* rays of query jobs with host buffers */
+} PbrtBatchLimits;
+
+/* Launch choices of a batch (the autotuner's search space). */
+typedef struct PbrtBatchTuning {
+    int32_t extend_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and query rays */
+    int32_t shadow_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: shadow rays */
+    uint32_t block;         /* threads per block: 128 or 256 */
+    uint32_t stack;         /* 4-wide kernels: shared-memory stack entries per ray, 8 or 16 */
+    uint32_t chunk;         /* rays a warp takes from the work counter at a time: 32..4096, multiple of 32 */
+    uint32_t refill;        /* extend: refill a warp when this many lanes are idle, 1..32 */
+    uint32_t refill_shadow; /* shadow: same, 1..32 */
+    uint32_t use_graph;     /* 1: replay the stage sequence as one CUDA graph */
+} PbrtBatchTuning;
+
+typedef struct PbrtBatchStats {
+    uint32_t jobs;
+    uint32_t kernels;       /* kernels of the last launch */
+    uint64_t samples, light_samples, film_pixels, query_rays;
+    uint32_t graph;         /* the last launch replayed a graph */
+    uint32_t pad;
+} PbrtBatchStats;
+
+typedef struct PbrtBatch PbrtBatch;
+
+int pbrtgpu_batch_bytes(const PbrtBatchLimits* limits, uint64_t* device_bytes, uint64_t* pinned_bytes);
+int pbrtgpu_batch_create(const PbrtBatchLimits* limits, PbrtBatch** out);
+void pbrtgpu_batch_destroy(PbrtBatch* batch);
+/* Adds a render; rgb_out as for pbrtgpu_render.  *job (may be NULL) gets its index. */
+int pbrtgpu_batch_add_render(PbrtBatch* batch, const PbrtScene* scene, const PbrtCameraDesc* camera,
+                             const PbrtSamplerDesc* sampler, float* rgb_out, uint32_t* job);
+/* Adds a ray query: closest hits into `hits`, or (hits NULL) any hit into
+ * `occluded`; host or device buffers. */
+int pbrtgpu_batch_add_query(PbrtBatch* batch, const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
+                            PbrtHit* hits, uint8_t* occluded, uint32_t* job);
+int pbrtgpu_batch_launch(PbrtBatch* batch, void* stream);
+/* 1 in *done once the last launch has finished (does not wait). */
+int pbrtgpu_batch_poll(PbrtBatch* batch, int32_t* done);
+/* Waits for the last launch, finishes host outputs, writes each job's status
+ * to job_status[job] (may be NULL) and empties the batch; returns the first
+ * failing job's status.  Without a launch since the jobs were added it only
+ * empties the batch. */
+int pbrtgpu_batch_wait(PbrtBatch* batch, int32_t* job_status);
+int pbrtgpu_batch_set_tuning(PbrtBatch* batch, const PbrtBatchTuning* tuning);
+int pbrtgpu_batch_get_tuning(const PbrtBatch* batch, PbrtBatchTuning* tuning);
+int pbrtgpu_batch_stats(const PbrtBatch* batch, PbrtBatchStats* stats);
+/* Times the jobs now in the batch under each candidate tuning (coordinate
+ * descent over kernel, block, stack, chunk, refill and graph choices,
+ * `repeats` launches each, CUDA events on `stream`), keeps the fastest and
+ * returns it with its time.  The jobs stay in the batch; their outputs are
+ * written by every trial (with the same values). */
+int pbrtgpu_batch_autotune(PbrtBatch* batch, void* stream, uint32_t repeats, PbrtBatchTuning* best,
+                           float* best_ms);
+
 /* Pixel extent (x0, x1, y0, y1) of the film a camera describes
  * (Film::get_pixel_extent, src/camera/film.rs:301-309). */
 int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* camera, int32_t ext[4]);

@@ -99,6 +99,26 @@ class PbrtTraceConfig(C.Structure):
 TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3}
 
 
+class PbrtBatchLimits(C.Structure):
+    _fields_ = [("max_jobs", C.c_uint32), ("max_tasks", C.c_uint32), ("max_samples", C.c_uint64),
+                ("max_light_samples", C.c_uint64), ("max_film_pixels", C.c_uint64), ("max_query_rays", C.c_uint64)]
+
+
+class PbrtBatchTuning(C.Structure):
+    _fields_ = [("extend_kernel", C.c_int32), ("shadow_kernel", C.c_int32), ("block", C.c_uint32),
+                ("stack", C.c_uint32), ("chunk", C.c_uint32), ("refill", C.c_uint32), ("refill_shadow", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class PbrtBatchStats(C.Structure):
+    _fields_ = [("jobs", C.c_uint32), ("kernels", C.c_uint32), ("samples", C.c_uint64),
+                ("light_samples", C.c_uint64), ("film_pixels", C.c_uint64), ("query_rays", C.c_uint64),
+                ("graph", C.c_uint32), ("pad", C.c_uint32)]
+
+
 class PbrtPackedNode(C.Structure):
     _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("is_leaf", C.c_int32), ("offset", C.c_uint32),
                 ("count", C.c_uint32)]
@@ -137,6 +157,19 @@ SIGNATURES = {
                                        C.c_uint32, _P, _P]),
     "pbrtgpu_render_noalloc": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
     "pbrtgpu_film_pixel_extent": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_int32)]),
+    "pbrtgpu_batch_bytes": (C.c_int, [C.POINTER(PbrtBatchLimits), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "pbrtgpu_batch_create": (C.c_int, [C.POINTER(PbrtBatchLimits), C.POINTER(C.c_void_p)]),
+    "pbrtgpu_batch_destroy": (None, [_P]),
+    "pbrtgpu_batch_add_render": (C.c_int, [_P, _P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P,
+                                           C.POINTER(C.c_uint32)]),
+    "pbrtgpu_batch_add_query": (C.c_int, [_P, _P, _P, C.c_uint32, _P, _P, C.POINTER(C.c_uint32)]),
+    "pbrtgpu_batch_launch": (C.c_int, [_P, _P]),
+    "pbrtgpu_batch_poll": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "pbrtgpu_batch_wait": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "pbrtgpu_batch_set_tuning": (C.c_int, [_P, C.POINTER(PbrtBatchTuning)]),
+    "pbrtgpu_batch_get_tuning": (C.c_int, [_P, C.POINTER(PbrtBatchTuning)]),
+    "pbrtgpu_batch_stats": (C.c_int, [_P, C.POINTER(PbrtBatchStats)]),
+    "pbrtgpu_batch_autotune": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(PbrtBatchTuning), C.POINTER(C.c_float)]),
 }
 
 _lib = None

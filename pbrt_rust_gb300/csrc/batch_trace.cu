@@ -1,0 +1,227 @@
+// batch_trace.cu - the traversal stages of the batched wavefront.
+//
+// extend: closest hit (renders, closest-hit queries) or any hit (any-hit
+//         queries) of every ray of every job
+// shadow: any hit of every queued shadow ray of every render job
+// Both are persistent kernels: a grid of resident warps takes `chunk` rays
+// at a time from a device work counter and refills a warp's idle lanes once
+// `refill` of them are idle, each lane finding its ray's job (and so its
+// scene's BVH and its output) by a binary search over the job offsets.
+// Each ray's traversal is the single-scene kernels' (trace.cuh,
+// trace4.cuh), so results are the same bit for bit.
+#include <cuda_runtime.h>
+
+#include "batch.h"
+#include "kernels.h"
+#include "trace.cuh"
+#include "trace4.cuh"
+
+namespace pbrt {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Cursor {
+    uint32_t j;
+    uint64_t lo, hi;
+};
+
+// Job of item g: the j with off[j] <= g < off[j + 1] (empty jobs have
+// off[j] == off[j + 1] and are never returned); the last answer is reused
+// while g stays inside it.
+__device__ __forceinline__ uint32_t locate(const uint64_t* __restrict__ off, uint32_t n, uint64_t g, Cursor& c) {
+    if (g >= c.lo && g < c.hi) return c.j;
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    c.j = lo;
+    c.lo = __ldg(off + lo);
+    c.hi = __ldg(off + lo + 1);
+    return lo;
+}
+
+// The chunked work source of one warp; every member call is warp-uniform.
+struct WorkSource {
+    uint64_t next = 0, end = 0;
+    bool more = true;
+
+    __device__ __forceinline__ void fetch(uint32_t* counter, uint32_t chunk, uint64_t n, unsigned lane) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, chunk);
+        base = __shfl_sync(kFull, base, 0);
+        if ((uint64_t)base < n) {
+            next = base;
+            end = (uint64_t)base + chunk < n ? (uint64_t)base + chunk : n;
+        } else {
+            more = false;
+        }
+    }
+};
+
+// Which hit the extend stage looks for: closest for every ray, any for
+// every ray, or each job's own choice.
+enum { kClosest = 0, kAny = 1, kPerJob = 2 };
+
+template <bool WIDE, int S1, int S2>
+struct Walker;  // traversal state over one layout
+
+template <int SMAX, int OVF>
+struct Walker<true, SMAX, OVF> {
+    Traversal4<SMAX, OVF> T;
+    DevBVH4 bv;
+    __device__ __forceinline__ void bind(uint2* smem) { T.bind(smem, threadIdx.x, blockDim.x); }
+    __device__ __forceinline__ bool start(const RenderParams& P, const DRay& r) {
+        bv = P.bvh4;
+        return T.start(bv, r);
+    }
+    template <int MODE>
+    __device__ __forceinline__ bool step(const DRay& r, bool any) {
+        if (MODE == kClosest) return T.template step<false>(bv, r);
+        if (MODE == kAny) return T.template step<true>(bv, r);
+        return any ? T.template step<true>(bv, r) : T.template step<false>(bv, r);
+    }
+    __device__ __forceinline__ int failure() const { return T.overflow ? 6 : 0; }
+    __device__ __forceinline__ bool found() const { return T.found; }
+    __device__ __forceinline__ const TraceResult& res() const { return T.res; }
+};
+
+template <int STACK, int UNUSED>
+struct Walker<false, STACK, UNUSED> {
+    Traversal<STACK> T;
+    DevBVH bv;
+    int st = 0;
+    __device__ __forceinline__ void bind(uint2*) {}
+    __device__ __forceinline__ bool start(const RenderParams& P, const DRay& r) {
+        bv = P.bvh;
+        return T.start(bv, r);
+    }
+    template <int MODE>
+    __device__ __forceinline__ bool step(const DRay& r, bool any) {
+        if (MODE == kClosest) return T.template step<false>(bv, r, &st);
+        if (MODE == kAny) return T.template step<true>(bv, r, &st);
+        return any ? T.template step<true>(bv, r, &st) : T.template step<false>(bv, r, &st);
+    }
+    __device__ __forceinline__ int failure() const { return st; }
+    __device__ __forceinline__ bool found() const { return T.found; }
+    __device__ __forceinline__ const TraceResult& res() const { return T.res; }
+};
+
+// SHADOW = false: extend over the job rays; true: the shadow queue (any
+// hit, MODE = kAny).
+template <int BLOCK, bool SHADOW, bool WIDE, int S1, int S2, int MODE>
+__global__ void __launch_bounds__(BLOCK) kb_trace(BatchArgs A) {
+    extern __shared__ uint2 smem_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nj = A.hdr->n_jobs;
+    const uint64_t n = SHADOW ? (uint64_t) * (volatile uint32_t*)(A.counters + kCtrShadowCount) : A.hdr->rays;
+    uint32_t* counter = A.counters + (SHADOW ? kCtrShadowWork : kCtrExtendWork);
+    const uint32_t refill = SHADOW ? A.refill_shadow : A.refill;
+    WorkSource W;
+    Cursor c{0, 1, 0};
+    Walker<WIDE, S1, S2> K;
+    K.bind(smem_stack);
+    DRay r;
+    bool busy = false, any = MODE == kAny;
+    uint32_t job = 0;
+    uint64_t item = 0;  // extend: index inside the job; shadow: queue entry
+    auto finish = [&]() {
+        const JobRec& J = A.jobs[job];
+        if (const int f = K.failure()) atomicMax((int*)(J.P.counters + 2), f);
+        if (SHADOW) {
+            J.P.occluded[__ldg(A.q_slot + item)] = K.found() ? 1 : 0;
+        } else if (any) {
+            J.occ[item] = K.found() ? 1 : 0;
+        } else {
+            const TraceResult& R = K.res();
+            J.hits[item] = make_float4(__int_as_float(R.prim), R.t, R.b1, R.b2);
+        }
+        busy = false;
+    };
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, !busy);
+        const unsigned nidle = __popc(idle);
+        if (W.more && W.next >= W.end && nidle >= refill) W.fetch(counter, A.chunk, n, lane);
+        const bool tail = !W.more && W.next + nidle >= W.end;
+        if (W.next < W.end && nidle >= (tail ? 1u : refill)) {
+            if (!busy) {
+                const uint64_t my = W.next + __popc(idle & ((1u << lane) - 1u));
+                if (my < W.end) {
+                    const float4* src;
+                    if (SHADOW) {
+                        job = __ldg(A.q_job + my);
+                        item = my;
+                        src = reinterpret_cast<const float4*>(A.q_rays) + 2 * my;
+                    } else {
+                        job = locate(A.off_ray, nj, my, c);
+                        item = my - c.lo;
+                        if (MODE == kPerJob) any = A.jobs[job].any != 0;
+                        src = A.jobs[job].rays + 2 * item;
+                    }
+                    r = make_dray(__ldg(src), __ldg(src + 1));
+                    busy = true;
+                    if (!K.start(A.jobs[job].P, r)) finish();
+                }
+            }
+            W.next += nidle;
+        }
+        if (!__any_sync(kFull, busy)) {
+            if (W.next >= W.end && !W.more) break;
+            continue;
+        }
+        if (busy && !K.template step<MODE>(r, any)) finish();
+    }
+}
+
+template <int BLOCK, bool SHADOW, bool WIDE, int S1, int S2, int MODE>
+cudaError_t go(const BatchArgs& A, int sms, cudaStream_t s) {
+    static int bps = 0;
+    const size_t smem = WIDE ? (size_t)S1 * sizeof(uint2) * BLOCK : 0;
+    if (bps == 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bps, kb_trace<BLOCK, SHADOW, WIDE, S1, S2, MODE>, BLOCK, smem);
+        if (e != cudaSuccess) return e;
+        if (bps < 1) bps = 1;
+    }
+    kb_trace<BLOCK, SHADOW, WIDE, S1, S2, MODE><<<(unsigned)(sms * bps), BLOCK, smem, s>>>(A);
+    return cudaGetLastError();
+}
+
+template <int BLOCK, bool SHADOW, int MODE>
+cudaError_t pick(const BatchArgs& A, const BatchTuning& T, bool wide, uint32_t cover, int sms, cudaStream_t s) {
+    if (wide) {
+        if (T.smax == 8)
+            return cover <= 64 ? go<BLOCK, SHADOW, true, 8, 56, MODE>(A, sms, s)
+                               : go<BLOCK, SHADOW, true, 8, 248, MODE>(A, sms, s);
+        return cover <= 64 ? go<BLOCK, SHADOW, true, 16, 48, MODE>(A, sms, s)
+                           : go<BLOCK, SHADOW, true, 16, 240, MODE>(A, sms, s);
+    }
+    return cover <= 64 ? go<BLOCK, SHADOW, false, 64, 0, MODE>(A, sms, s)
+                       : go<BLOCK, SHADOW, false, 256, 0, MODE>(A, sms, s);
+}
+
+template <int BLOCK>
+cudaError_t pick_block(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool wide, uint32_t cover,
+                       int sms, cudaStream_t s) {
+    if (shadow) return pick<BLOCK, true, kAny>(A, T, wide, cover, sms, s);
+    return mixed ? pick<BLOCK, false, kPerJob>(A, T, wide, cover, sms, s)
+                 : pick<BLOCK, false, kClosest>(A, T, wide, cover, sms, s);
+}
+
+}  // namespace
+
+cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed,
+                               uint32_t cover_pair, uint32_t cover_wide, int sms, cudaStream_t s) {
+    const bool wide = shadow ? T.shadow_wide : T.extend_wide;
+    const uint32_t cover = wide ? cover_wide : cover_pair;
+    if (cover > 256) return cudaErrorInvalidValue;
+    if (T.block == 256) return pick_block<256>(A, T, shadow, mixed, wide, cover, sms, s);
+    return pick_block<128>(A, T, shadow, mixed, wide, cover, sms, s);
+}
+
+}  // namespace pbrt

@@ -85,10 +85,16 @@ struct PbrtScene {
 };
 
 namespace pbrt {
+// Validates a render's descriptors, uploads the scene on first use and fills
+// every field of *out except the filter table, the task array and the
+// per-render buffers (capi_render.cu).
+int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp, uint32_t task_lo,
+                   uint32_t task_hi, RenderParams* out, std::vector<TaskRec>* tasks);
 // Render set-up helpers (capi_render.cu), the reference's f32 arithmetic.
 int32_t f2i32(float f);
 size_t f2usize(float f);
 void crop_window(size_t num, size_t count, float aspect, float out[4]);
+void gather_offsets(float filter_width, int32_t sampler_start, int32_t sampler_end, int32_t* lo, int32_t* hi);
 void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]);
 void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[4]);
 void chacha_key(uint64_t state, uint32_t key[8]);

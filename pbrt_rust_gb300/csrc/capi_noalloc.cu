@@ -123,7 +123,8 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     P.filter_yw = cam->filter_y_width;
     P.filter_inv_xw = 1.0f / cam->filter_x_width;
     P.filter_inv_yw = 1.0f / cam->filter_y_width;
-    P.gather_radius = (int32_t)std::ceil(std::max(cam->filter_x_width, cam->filter_y_width)) + 1;
+    gather_offsets(cam->filter_x_width, P.sx0, P.sx1, &P.gx0, &P.gx1);
+    gather_offsets(cam->filter_y_width, P.sy0, P.sy1, &P.gy0, &P.gy1);
 
     // task table and box filter table on the host stack (no heap use)
     TaskRec tasks[kNoAllocMaxTasks];

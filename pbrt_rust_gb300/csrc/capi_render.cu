@@ -100,6 +100,25 @@ void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[
     ext[3] = ys + yc;
 }
 
+// Source pixels whose samples can land on film pixel p, along one axis:
+// p + [*lo, *hi].  A sample of source pixel s lies at a position v in
+// [s, s + 1], and it lands on p only if ceil(v - 0.5 - w) <= p <=
+// floor(v - 0.5 + w) (film.rs:198-210), i.e. v in [p + 0.5 - w, p + 0.5 + w]
+// up to the f32 rounding of those sums, which stays below 1/16 for sample
+// coordinates under 2^20.  Hence s in [p + ceil(-0.5 - w - 1/16),
+// p + floor(0.5 + w + 1/16)]: 3 source pixels per axis for the box filter
+// of radius 0.5.  Windows reaching beyond 2^20 take a wider margin.
+void gather_offsets(float w, int32_t s0, int32_t s1, int32_t* lo, int32_t* hi) {
+    const int32_t big = 1 << 20;
+    if (s0 > -big && s1 < big) {
+        *lo = (int32_t)std::ceil(-0.5f - w - 0.0625f);
+        *hi = (int32_t)std::floor(0.5f + w + 0.0625f);
+    } else {
+        *lo = -((int32_t)std::ceil(w) + 2);
+        *hi = (int32_t)std::ceil(w) + 2;
+    }
+}
+
 // rand_core 0.6.4 SeedableRng::seed_from_u64 (the published PCG32 seed
 // expansion: multiplier 6364136223846793005, increment
 // 11634580027462260723, XSH-RR output, state advanced before output).
@@ -301,10 +320,17 @@ int pbrtgpu_render(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSam
     return pbrtgpu_render_tasks(cS, cam, smp, 0, smp->num_tasks, rgb_out, stream_v);
 }
 
-int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp,
-                         uint32_t task_lo, uint32_t task_hi, float* rgb_out, void* stream_v) {
-    PbrtScene* S = const_cast<PbrtScene*>(cS);
-    if (!S || !cam || !smp || !rgb_out) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+}  // extern "C"
+
+namespace pbrt {
+
+// Validates a render's descriptors, uploads the scene on first use and fills
+// every field of *out except the filter table, the task array and the
+// per-render buffers; *tasks gets the task records (tasks outside
+// [task_lo, task_hi) empty).
+int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp, uint32_t task_lo,
+                   uint32_t task_hi, RenderParams* out, std::vector<TaskRec>* tasks_out) {
+    if (!S || !cam || !smp) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (smp->num_tasks == 0) return set_error(PBRT_ERR_INVALID_ARGUMENT, "num_tasks must be > 0");
     if (task_lo > task_hi || task_hi > smp->num_tasks)
         return set_error(PBRT_ERR_INVALID_ARGUMENT, "task range must satisfy task_lo <= task_hi <= num_tasks");
@@ -318,9 +344,6 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
         return set_error(PBRT_ERR_INVALID_ARGUMENT, "filter width must be in (0, 16]");
     int st;
     if (!S->uploaded && (st = scene_upload(S))) return st;
-    DeviceGuard g(S->bvh->device);
-    std::lock_guard<std::mutex> lk(S->mu);
-    cudaStream_t s = (cudaStream_t)stream_v;
     const uint32_t nl = (uint32_t)S->lights.size();
 
     RenderParams P;
@@ -351,7 +374,8 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
     P.filter_yw = cam->filter_y_width;
     P.filter_inv_xw = 1.0f / cam->filter_x_width;
     P.filter_inv_yw = 1.0f / cam->filter_y_width;
-    P.gather_radius = (int32_t)std::ceil(std::max(cam->filter_x_width, cam->filter_y_width)) + 1;
+    gather_offsets(cam->filter_x_width, P.sx0, P.sx1, &P.gx0, &P.gx1);
+    gather_offsets(cam->filter_y_width, P.sy0, P.sy1, &P.gy0, &P.gy1);
 
     // tasks (sampler_renderer.rs:61-75, film.rs:124-147)
     std::vector<TaskRec> tasks(smp->num_tasks);
@@ -381,6 +405,39 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
         T.fy0 = std::max(te[2], P.fy0);
         T.fy1 = std::min(te[3], P.fy1);
     }
+    P.bvh = S->bvh->dev;
+    P.depth = S->bvh->host.depth;
+    P.bvh4 = S->bvh->dev4;
+    P.wide_bound = S->bvh->host.stack4_bound;
+    P.has_wide = wide_of(S->bvh) ? 1u : 0u;
+    P.shade = S->d_shade;
+    P.spheres = S->bvh->d_spheres;
+    P.materials = S->d_materials;
+    P.lights = S->d_lights;
+    P.n_lights = nl;
+    P.area_tris = S->d_area_tris;
+    P.area_cdf = S->d_area_cdf;
+    *out = P;
+    *tasks_out = std::move(tasks);
+    return PBRT_OK;
+}
+
+}  // namespace pbrt
+
+extern "C" {
+
+int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp,
+                         uint32_t task_lo, uint32_t task_hi, float* rgb_out, void* stream_v) {
+    PbrtScene* S = const_cast<PbrtScene*>(cS);
+    if (!S || !cam || !smp || !rgb_out) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    RenderParams P;
+    std::vector<TaskRec> tasks;
+    int st = prepare_render(S, cam, smp, task_lo, task_hi, &P, &tasks);
+    if (st) return st;
+    DeviceGuard g(S->bvh->device);
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaStream_t s = (cudaStream_t)stream_v;
+    const uint32_t nl = P.n_lights;
     // box filter table (film.rs:89-97): Filter::mean evaluates to 1
     std::vector<float> table(256, 1.0f);
 
@@ -404,18 +461,6 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
     P.filter_table = (const float*)S->table.p;
     P.tasks = (const TaskRec*)S->tasks.p;
     P.n_tasks = smp->num_tasks;
-    P.bvh = S->bvh->dev;
-    P.depth = S->bvh->host.depth;
-    P.bvh4 = S->bvh->dev4;
-    P.wide_bound = S->bvh->host.stack4_bound;
-    P.has_wide = wide_of(S->bvh) ? 1u : 0u;
-    P.shade = S->d_shade;
-    P.spheres = S->bvh->d_spheres;
-    P.materials = S->d_materials;
-    P.lights = S->d_lights;
-    P.n_lights = nl;
-    P.area_tris = S->d_area_tris;
-    P.area_cdf = S->d_area_cdf;
     P.rays = (PbrtRay*)S->rays.p;
     P.hits = (float4*)S->hits.p;
     P.img = (float2*)S->img.p;

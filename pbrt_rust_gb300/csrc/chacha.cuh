@@ -78,6 +78,16 @@ struct WordStream {
         idx = (int)(word & 15);
         chacha12_block(key, block, buf);
     }
+    // Moves n words ahead without reading them.
+    __device__ __forceinline__ void skip(uint32_t n) {
+        const uint64_t pos = block * 16u + (uint64_t)idx + n;
+        const uint64_t nb = pos >> 4;
+        idx = (int)(pos & 15u);
+        if (nb != block) {
+            block = nb;
+            chacha12_block(key, block, buf);
+        }
+    }
     __device__ __forceinline__ uint32_t next_u32() {
         if (idx == 16) {
             ++block;

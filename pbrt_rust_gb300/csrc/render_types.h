@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 
+#include "../../include/pbrt_gpu.h"
 #include "layout.h"
 #include "trace.cuh"
 #include "trace4.cuh"
@@ -59,7 +60,9 @@ struct RenderParams {
     // film (camera/film.rs)
     int32_t fx0, fx1, fy0, fy1;  // main film pixel extent
     float filter_xw, filter_yw, filter_inv_xw, filter_inv_yw;
-    int32_t gather_radius;
+    // film pixel p gathers the samples of source pixels p + [g*0, g*1]
+    // (gather_offsets in capi_render.cu)
+    int32_t gx0, gx1, gy0, gy1;
     const float* filter_table;   // 16 x 16
     // tasks
     const TaskRec* tasks;

@@ -235,3 +235,45 @@ def heightfield(n_side: int = 708, seed: int | None = None, res: int = 1024, spp
     hi = pts.max(axis=0).astype(np.float64) + 1.0
     rays = incoherent_rays(rng, n_rays, lo, hi) if n_rays else None
     return prims, lights, camera, sampler, rays
+
+
+def multi_scene(index: int, seed: int | None = None, tri_range=(1000, 256000), res_choices=(128, 256, 512),
+                spp_choices=(1, 4, 16), max_spheres: int = 32):
+    """One scene of the batched multi-scene workload: a random-triangle soup
+    (as in ray_soup) with a log-uniform triangle count in tri_range, scaled
+    to an extent E ~ U[1, 4]; 0..max_spheres matte spheres (r ~ E * U[0.05,
+    0.2], centre ~ U[-E, E]^3); matte Kd ~ U[0.2, 0.8]^3 throughout; a point
+    light (intensity 50 E^2 at (0, 2E, -E)) and a 1E x 1E quad area light at
+    y = 1.5E facing down (L = 10).  Camera at (0, 0.5E, -3.5E) looking at the
+    origin, fov 60; resolution and spp drawn from the choices (spp as n x n
+    jittered strata).  Returns (prims, lights, camera, sampler)."""
+    rng = PCG32(config_seed(3, index) if seed is None else seed)
+    u = rng.uniform(8)
+    lo, hi = math.log(tri_range[0]), math.log(tri_range[1])
+    n_tris = int(round(math.exp(lo + (hi - lo) * u[0])))
+    E = 1.0 + 3.0 * u[1]
+    n_sph = min(int(u[2] * (max_spheres + 1)), max_spheres)
+    res = res_choices[min(int(u[3] * len(res_choices)), len(res_choices) - 1)]
+    spp = spp_choices[min(int(u[4] * len(spp_choices)), len(spp_choices) - 1)]
+    side = int(round(math.sqrt(spp)))
+    kd = tuple(0.2 + 0.6 * u[5:8])
+    pts, idx = random_triangle_soup(rng, n_tris, extent=E, offset=0.05 * E)
+    mesh = Shape.triangle_mesh(Transform(), None, False, idx, pts)
+    prims = [Primitive.geometric(mesh, MatteMaterial(kd))]
+    s = rng.uniform(7 * n_sph).reshape(n_sph, 7) if n_sph else np.zeros((0, 7))
+    for i in range(n_sph):
+        r = E * (0.05 + 0.15 * s[i, 0])
+        c = tuple(E * (2.0 * s[i, 1:4] - 1.0))
+        o2w = Transform.translate(c)
+        prims.append(Primitive.geometric(Shape.sphere(o2w, o2w.inverse(), False, r, -r, r, 360.0),
+                                         MatteMaterial(tuple(0.2 + 0.6 * s[i, 4:7]))))
+    lights = [PointLight(Transform.translate((0.0, 2.0 * E, -E)), (50.0 * E * E,) * 3)]
+    area = DiffuseAreaLight(Transform(), (10.0, 10.0, 10.0))
+    prims.append(Primitive.geometric_area_light(quad_light_mesh((0.0, 1.5 * E, 0.0), E), MatteMaterial((0, 0, 0)),
+                                                area))
+    lights.append(area)
+    cam2world = Transform.look_at((0.0, 0.5 * E, -3.5 * E), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0)).inverse()
+    film = Film.image(res, res, Filter.mean(0.5, 0.5))
+    camera = Camera.perspective(cam2world, (-1.0, 1.0, -1.0, 1.0), 0.0, 1.0, 0.0, 1e30, 60.0, film)
+    sampler = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
+    return prims, lights, camera, sampler
