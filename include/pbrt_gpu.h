@@ -364,6 +364,56 @@ int pbrtgpu_batch_stats(const PbrtBatch* batch, PbrtBatchStats* stats);
 int pbrtgpu_batch_autotune(PbrtBatch* batch, void* stream, uint32_t repeats, PbrtBatchTuning* best,
                            float* best_ms);
 
+/* ---- serving loop ----------------------------------------------------
+ * No counterpart in the reference (a one-shot renderer).  A server keeps
+ * scenes resident (the caller's PbrtScene / PbrtBVH handles), accepts render
+ * and ray-query requests from any host thread, and runs them with
+ * continuous batching: a worker thread packs the requests waiting in arrival
+ * order into the first free batch slot - as many as fit the slot's device
+ * memory limits - and launches it at once, so requests that arrive while
+ * other batches run on the device are admitted as slots free up, and up to
+ * `slots` batches are in flight together (each on its own stream).  A
+ * request larger than a slot's limits is refused at submission with
+ * PBRT_ERR_BUDGET.  Each result equals what the single-request entry point
+ * gives (bit for bit), alone or in any mix. */
+typedef struct PbrtServerConfig {
+    uint32_t slots;          /* batches in flight at once, 1..8 */
+    uint32_t use_tuning;     /* 1: apply `tuning` to every slot */
+    PbrtBatchLimits limits;  /* device memory of each slot (pbrtgpu_batch_bytes) */
+    PbrtBatchTuning tuning;
+} PbrtServerConfig;
+
+typedef struct PbrtServerStats {
+    uint64_t submitted, completed, failed, batches;
+    double mean_batch_requests;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submission to result, completed requests */
+    double span_s;                           /* first submission to last result */
+    double requests_per_s;                   /* completed / span_s */
+} PbrtServerStats;
+
+typedef struct PbrtServer PbrtServer;
+
+int pbrtgpu_server_create(const PbrtServerConfig* config, PbrtServer** out);
+/* Finishes every submitted request, then frees the server. */
+void pbrtgpu_server_destroy(PbrtServer* server);
+/* The camera and sampler descriptions are copied; the scene, rgb_out and
+ * (for queries) the rays and outputs must stay valid until the request has
+ * completed.  *ticket identifies the request. */
+int pbrtgpu_server_submit_render(PbrtServer* server, const PbrtScene* scene, const PbrtCameraDesc* camera,
+                                 const PbrtSamplerDesc* sampler, float* rgb_out, uint64_t* ticket);
+int pbrtgpu_server_submit_query(PbrtServer* server, const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
+                                PbrtHit* hits, uint8_t* occluded, uint64_t* ticket);
+/* Waits until the request has completed (timeout_s < 0: no limit) and
+ * forgets it; *status gets its PbrtStatus.  PBRT_ERR_CANCELLED if the
+ * timeout passed first (the request stays queued), PBRT_ERR_INVALID_ARGUMENT
+ * for an unknown ticket. */
+int pbrtgpu_server_wait(PbrtServer* server, uint64_t ticket, double timeout_s, int32_t* status);
+/* Waits until every submitted request has completed. */
+int pbrtgpu_server_drain(PbrtServer* server);
+int pbrtgpu_server_stats(PbrtServer* server, PbrtServerStats* stats);
+/* Forgets the latency record (completed requests stay waitable). */
+int pbrtgpu_server_reset_stats(PbrtServer* server);
+
 /* Pixel extent (x0, x1, y0, y1) of the film a camera describes
  * (Film::get_pixel_extent, src/camera/film.rs:301-309). */
 int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* camera, int32_t ext[4]);

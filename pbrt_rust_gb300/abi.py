@@ -113,6 +113,18 @@ class PbrtBatchTuning(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class PbrtServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("use_tuning", C.c_uint32), ("limits", PbrtBatchLimits),
+                ("tuning", PbrtBatchTuning)]
+
+
+class PbrtServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("batches", C.c_uint64), ("mean_batch_requests", C.c_double), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
+                ("requests_per_s", C.c_double)]
+
+
 class PbrtBatchStats(C.Structure):
     _fields_ = [("jobs", C.c_uint32), ("kernels", C.c_uint32), ("samples", C.c_uint64),
                 ("light_samples", C.c_uint64), ("film_pixels", C.c_uint64), ("query_rays", C.c_uint64),
@@ -170,6 +182,15 @@ SIGNATURES = {
     "pbrtgpu_batch_get_tuning": (C.c_int, [_P, C.POINTER(PbrtBatchTuning)]),
     "pbrtgpu_batch_stats": (C.c_int, [_P, C.POINTER(PbrtBatchStats)]),
     "pbrtgpu_batch_autotune": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(PbrtBatchTuning), C.POINTER(C.c_float)]),
+    "pbrtgpu_server_create": (C.c_int, [C.POINTER(PbrtServerConfig), C.POINTER(C.c_void_p)]),
+    "pbrtgpu_server_destroy": (None, [_P]),
+    "pbrtgpu_server_submit_render": (C.c_int, [_P, _P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P,
+                                               C.POINTER(C.c_uint64)]),
+    "pbrtgpu_server_submit_query": (C.c_int, [_P, _P, _P, C.c_uint32, _P, _P, C.POINTER(C.c_uint64)]),
+    "pbrtgpu_server_wait": (C.c_int, [_P, C.c_uint64, C.c_double, C.POINTER(C.c_int32)]),
+    "pbrtgpu_server_drain": (C.c_int, [_P]),
+    "pbrtgpu_server_stats": (C.c_int, [_P, C.POINTER(PbrtServerStats)]),
+    "pbrtgpu_server_reset_stats": (C.c_int, [_P]),
 }
 
 _lib = None

@@ -277,3 +277,14 @@ def multi_scene(index: int, seed: int | None = None, tri_range=(1000, 256000), r
     camera = Camera.perspective(cam2world, (-1.0, 1.0, -1.0, 1.0), 0.0, 1.0, 0.0, 1e30, 60.0, film)
     sampler = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
     return prims, lights, camera, sampler
+
+
+def orbit_camera(camera, radius: float, azimuth: float, height: float | None = None, target=(0.0, 0.0, 0.0)):
+    """The camera moved to a point on a circle around `target` (radius,
+    azimuth in radians, height above the target: radius / 4 by default),
+    looking at the target; film, fov and screen window unchanged."""
+    h = radius / 4.0 if height is None else height
+    eye = (target[0] + radius * math.sin(azimuth), target[1] + h, target[2] - radius * math.cos(azimuth))
+    cam2world = Transform.look_at(eye, tuple(target), (0.0, 1.0, 0.0)).inverse()
+    return Camera.perspective(cam2world, camera.screen_window, camera.shutter_open, camera.shutter_close,
+                              camera.lens_radius, camera.focal_distance, camera.fov, camera.film)
