@@ -169,6 +169,156 @@ def algorithmic_bytes_per_ray(ob, rays, sample: int = 1 << 16):
     return 32.0 * nodes + 48.0 * tris + 32.0 + 16.0, nodes, tris
 
 
+def build_multi_scene(n: int, threads: int = 8):
+    """The batched multi-scene workload: n scenes of 1k-256k triangles (log
+    uniform) + 0-32 spheres, 128/256/512 squared at 1/4/16 spp."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from pbrt_rust_gb300 import generators as G
+    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
+
+    def one(i):
+        prims, lights, cam, smp = G.multi_scene(i)
+        return GpuScene(prims, lights), GpuSamplerRenderer(smp, cam)
+
+    with ThreadPoolExecutor(threads) as ex:  # host BVH builds release the GIL
+        return list(ex.map(one, range(n)))
+
+
+def bench_batched(torch, dev, stream, n_scenes: int = 64):
+    """Renders/s of n_scenes renders: one pbrtgpu_render per scene in turn
+    (the plain one-scene-per-launch path) against one autotuned batch."""
+    from pbrt_rust_gb300.batch import GpuBatch
+    items = build_multi_scene(n_scenes)
+    outs = [torch.empty((r.camera.film.y_res, r.camera.film.x_res, 3), device=dev) for _, r in items]
+    samples = sum(r.camera.film.x_res * r.camera.film.y_res * r.sampler.x_samples * r.sampler.y_samples
+                  for _, r in items)
+    film = sum(r.camera.film.x_res * r.camera.film.y_res for _, r in items)
+    for (sc, r), o in zip(items, outs):  # warm-up: uploads, scratch
+        r.render(sc, out=o, stream=stream)
+    torch.cuda.synchronize(dev)
+    reps = 2
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for (sc, r), o in zip(items, outs):
+            r.render(sc, out=o, stream=stream)
+    torch.cuda.synchronize(dev)
+    plain_s = (time.perf_counter() - t0) / reps
+    ref = [o.clone() for o in outs]
+    b = GpuBatch(max_jobs=n_scenes, max_tasks=64 * n_scenes, max_samples=samples, max_light_samples=2 * samples,
+                 max_film_pixels=film)
+    bouts = [torch.empty_like(o) for o in outs]
+    for (sc, r), o in zip(items, bouts):
+        b.add_render(sc, r, out=o)
+    tuned, tuned_ms = b.autotune(stream=stream, repeats=2)
+    b.wait()
+    times = []
+    for _ in range(3):
+        for (sc, r), o in zip(items, bouts):
+            b.add_render(sc, r, out=o)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        b.launch(stream)
+        b.wait()
+        times.append(time.perf_counter() - t0)
+    stats = b.stats()
+    exact = all(torch.equal(a.view(torch.int32), c.view(torch.int32)) for a, c in zip(bouts, ref))
+    if not exact:
+        raise RuntimeError("batched renders differ from the one-scene renders")
+    batch_s = statistics.median(times)
+    return {"scenes": n_scenes, "samples": samples, "plain_renders_per_s": n_scenes / plain_s,
+            "batched_renders_per_s": n_scenes / batch_s, "speedup": plain_s / batch_s,
+            "batched_ms": 1e3 * batch_s, "plain_ms": 1e3 * plain_s, "autotuned": tuned,
+            "kernels_per_launch": stats["kernels"], "graph": bool(stats["graph"]), "bit_exact": exact}
+
+
+def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 400, rate: float = 1000.0):
+    """Requests/s and latency of the serving loop against the plain path
+    (one request at a time through pbrtgpu_render / pbrtgpu_intersect) on
+    the same request stream; all outputs device-resident."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from pbrt_rust_gb300 import generators as G
+    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
+    from pbrt_rust_gb300.scene import Camera, Film, Filter, StratifiedSampler
+    from pbrt_rust_gb300.server import GpuServer
+
+    def one(i):
+        prims, lights, cam, smp = G.multi_scene(i, seed=G.config_seed(4, i), tri_range=(10000, 1000000),
+                                                res_choices=(128,), spp_choices=(1,))
+        sc = GpuScene(prims, lights)
+        return sc, sc.aggregate(), cam
+
+    with ThreadPoolExecutor(8) as ex:
+        pool = list(ex.map(one, range(n_scenes)))
+    reqs = []
+    for spec in G.serving_requests(n_requests, n_scenes):
+        sc, bvh, cam = pool[spec["scene"]]
+        if spec["kind"] == "render":
+            res, side = spec["res"], 1 if spec["spp"] == 1 else 2
+            film = Film.image(res, res, Filter.mean(0.5, 0.5))
+            c = G.orbit_camera(Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, 60.0,
+                                                  film), spec["radius"], spec["azimuth"])
+            smp = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
+            reqs.append(("render", sc, GpuSamplerRenderer(smp, c), torch.empty((res, res, 3), device=dev)))
+        else:
+            lo, hi = bvh.world_bound()
+            rays = G.incoherent_rays(G.PCG32(spec["seed"]), spec["n"], lo, hi)
+            rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+            reqs.append(("query", bvh, rd, torch.empty((spec["n"], 4), device=dev)))
+
+    def plain(r):
+        if r[0] == "render":
+            r[2].render(r[1], out=r[3], stream=stream)  # returns after the frame is done
+        else:
+            r[1].intersect(r[2], out=r[3], stream=stream)
+            stream.synchronize()
+
+    for r in reqs[:20]:
+        plain(r)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for r in reqs:
+        plain(r)
+    plain_s = time.perf_counter() - t0
+    ref = [r[3].clone() for r in reqs]
+    srv = GpuServer(slots=2, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22, max_query_rays=1 << 20,
+                    max_tasks=1 << 14)
+    outs = [torch.empty_like(r[3]) for r in reqs]
+
+    def serve(arrivals=None):
+        srv.reset_stats()
+        tickets = []
+        t0 = time.perf_counter()
+        for k, (r, o) in enumerate(zip(reqs, outs)):
+            if arrivals is not None:
+                while time.perf_counter() - t0 < arrivals[k]:
+                    pass
+            tickets.append(srv.submit_render(r[1], r[2], out=o) if r[0] == "render"
+                           else srv.submit_query(r[1], r[2], out=o))
+        for t in tickets:
+            srv.wait(t)
+        return srv.stats()
+
+    serve()
+    flood = serve()
+    torch.cuda.synchronize(dev)
+    exact = all(torch.equal(a.view(torch.int32), b.view(torch.int32)) for a, b in zip(outs, ref))
+    if not exact:
+        raise RuntimeError("served results differ from the one-request results")
+    poisson = serve(G.poisson_arrivals(len(reqs), rate, seed=9))
+    srv.close()
+    n_render = sum(1 for r in reqs if r[0] == "render")
+    return {"scenes": n_scenes, "requests": len(reqs), "renders": n_render, "queries": len(reqs) - n_render,
+            "plain_requests_per_s": len(reqs) / plain_s, "served_requests_per_s": flood["requests_per_s"],
+            "speedup": flood["requests_per_s"] * plain_s / len(reqs),
+            "flood_p50_ms": flood["p50_ms"], "flood_p99_ms": flood["p99_ms"],
+            "flood_mean_batch": flood["mean_batch_requests"],
+            "poisson_rate": rate, "poisson_requests_per_s": poisson["requests_per_s"],
+            "poisson_p50_ms": poisson["p50_ms"], "poisson_p99_ms": poisson["p99_ms"],
+            "poisson_mean_batch": poisson["mean_batch_requests"], "bit_exact": exact}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -298,6 +448,8 @@ def run_ours(args):
         t0 = time.perf_counter()
         renderer.render(scene, out=img, stream=stream)
         rt.append(time.perf_counter() - t0)
+    batched = bench_batched(torch, dev, stream) if not args.skip_multi else None
+    served = bench_served(torch, dev, stream) if not args.skip_multi else None
     clk.__exit__(None, None, None)
 
     mean_ms = statistics.mean(ms_closest)
@@ -338,6 +490,8 @@ def run_ours(args):
             "render_1024x1024_16spp": {"ms_mean": 1e3 * statistics.mean(rt), "ms_min": 1e3 * min(rt),
                                        "camera_rays": 1024 * 1024 * 16},
             "bvh_host_build_s": build_s,
+            "batched_multi_scene": batched,
+            "served": served,
         }
         print(json.dumps(out))
     if ws > 1:
@@ -352,6 +506,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-multi", action="store_true", help="skip the batched and served sections")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

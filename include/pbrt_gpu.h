@@ -131,7 +131,20 @@ typedef struct PbrtCameraDesc {
     uint32_t x_res, y_res;
     float crop_window[4];
     float filter_x_width, filter_y_width;
+    /* Filter of the film (src/filter.rs:44-85): PBRT_FILTER_*, with
+     * p0 = alpha (gaussian), B (mitchell) or tau (lanczos) and
+     * p1 = C (mitchell). */
+    int32_t filter_kind;
+    float filter_p0, filter_p1;
 } PbrtCameraDesc;
+
+enum {
+    PBRT_FILTER_BOX = 0,      /* Filter::mean */
+    PBRT_FILTER_TRIANGLE = 1,
+    PBRT_FILTER_GAUSSIAN = 2,
+    PBRT_FILTER_MITCHELL = 3,
+    PBRT_FILTER_LANCZOS = 4
+};
 
 /* Stratified sampler (src/sampler/stratified.rs:23-37) and the task count
  * of SamplerRenderer (src/sampler_renderer.rs:39-44), given explicitly so
@@ -413,6 +426,21 @@ int pbrtgpu_server_drain(PbrtServer* server);
 int pbrtgpu_server_stats(PbrtServer* server, PbrtServerStats* stats);
 /* Forgets the latency record (completed requests stay waitable). */
 int pbrtgpu_server_reset_stats(PbrtServer* server);
+
+/* The film's 16 x 16 filter table (film.rs:89-97: the filter evaluated at
+ * ((i + 0.5) / 16) of its width), row-major by y; the table every render
+ * entry point uses for this camera. */
+int pbrtgpu_filter_table(const PbrtCameraDesc* camera, float table[256]);
+
+/* Film output (Film::write_image, src/camera/film.rs:316-354, and
+ * write_img, film.rs:15-33).  rgb: host memory, width * height RGB triples
+ * of linear float as the render entry points return them.  The format
+ * follows the file extension: .png / .ppm get 8-bit channels
+ * (255 * p^(1/2.2) + 0.5, clamped to [0, 255] and truncated, as write_img
+ * computes them), .pfm the linear floats.  pbrtgpu_image_bytes gives those
+ * 8-bit values without writing a file. */
+int pbrtgpu_write_image(const float* rgb, uint32_t width, uint32_t height, const char* path);
+int pbrtgpu_image_bytes(const float* rgb, uint32_t width, uint32_t height, uint8_t* out);
 
 /* Pixel extent (x0, x1, y0, y1) of the film a camera describes
  * (Film::get_pixel_extent, src/camera/film.rs:301-309). */

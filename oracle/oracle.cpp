@@ -1637,7 +1637,9 @@ void run_task(RenderCtx& R, uint32_t task, std::vector<float>* dump, uint64_t* s
     }
 }
 
-Filter camera_filter(const PbrtCameraDesc& c) { return filter_new(0, c.filter_x_width, c.filter_y_width, 0, 0); }
+Filter camera_filter(const PbrtCameraDesc& c) {
+    return filter_new(c.filter_kind, c.filter_x_width, c.filter_y_width, c.filter_p0, c.filter_p1);
+}
 
 }  // namespace
 

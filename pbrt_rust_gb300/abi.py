@@ -80,6 +80,7 @@ class PbrtCameraDesc(C.Structure):
         ("shutter_open", C.c_float), ("shutter_close", C.c_float),
         ("x_res", C.c_uint32), ("y_res", C.c_uint32), ("crop_window", C.c_float * 4),
         ("filter_x_width", C.c_float), ("filter_y_width", C.c_float),
+        ("filter_kind", C.c_int32), ("filter_p0", C.c_float), ("filter_p1", C.c_float),
     ]
 
 
@@ -97,6 +98,7 @@ class PbrtTraceConfig(C.Structure):
 
 
 TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3}
+FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "mitchell": 3, "lanczos": 4}
 
 
 class PbrtBatchLimits(C.Structure):
@@ -169,6 +171,9 @@ SIGNATURES = {
                                        C.c_uint32, _P, _P]),
     "pbrtgpu_render_noalloc": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
     "pbrtgpu_film_pixel_extent": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_int32)]),
+    "pbrtgpu_filter_table": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_float)]),
+    "pbrtgpu_write_image": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_char_p]),
+    "pbrtgpu_image_bytes": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P]),
     "pbrtgpu_batch_bytes": (C.c_int, [C.POINTER(PbrtBatchLimits), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "pbrtgpu_batch_create": (C.c_int, [C.POINTER(PbrtBatchLimits), C.POINTER(C.c_void_p)]),
     "pbrtgpu_batch_destroy": (None, [_P]),

@@ -32,8 +32,8 @@ size_t up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 struct Layout {
     size_t rays, hits, img, le, L;                  // per sample
     size_t lsamp, contrib, occ, qrays, qslot, qjob;  // per light sample
-    size_t table, counters;
-    size_t upload, o_pix, o_ray, o_smp, o_film, o_jobs, o_tasks, upload_bytes;
+    size_t counters;
+    size_t upload, o_pix, o_ray, o_smp, o_film, o_jobs, o_tables, o_tasks, upload_bytes;
     size_t st_rays, st_hits, st_occ, st_rgb;
     size_t total;
     size_t pinned;  // upload block + counters
@@ -57,15 +57,15 @@ struct Layout {
         qrays = take(SL * sizeof(PbrtRay));
         qslot = take(SL * 4);
         qjob = take(SL * 4);
-        table = take(256 * 4);
         counters = take((J + 1) * kCtrWords * 4);
-        // upload block: [hdr | 4 offset arrays | jobs | tasks]
+        // upload block: [hdr | 4 offset arrays | jobs | filter tables | tasks]
         o_pix = up(sizeof(BatchHdr));
         o_ray = o_pix + up((J + 1) * 8);
         o_smp = o_ray + up((J + 1) * 8);
         o_film = o_smp + up((J + 1) * 8);
         o_jobs = o_film + up((J + 1) * 8);
-        o_tasks = o_jobs + up(J * sizeof(JobRec));
+        o_tables = o_jobs + up(J * sizeof(JobRec));
+        o_tasks = o_tables + up(J * 256 * sizeof(float));
         upload_bytes = o_tasks + up((size_t)L0.max_tasks * sizeof(TaskRec));
         upload = take(upload_bytes);
         st_rays = take(Q * sizeof(PbrtRay));
@@ -251,7 +251,7 @@ int launch_locked(PbrtBatch* b, cudaStream_t s, bool timed) {
     H->film = b->n_film;
     int st;
     unsigned char* du = b->d + b->lay.upload;
-    if ((st = cuda_status(cudaMemcpyAsync(du, b->h, b->lay.o_jobs + (size_t)b->n_jobs * sizeof(JobRec),
+    if ((st = cuda_status(cudaMemcpyAsync(du, b->h, b->lay.o_tables + (size_t)b->n_jobs * 256 * sizeof(float),
                                           cudaMemcpyHostToDevice, s),
                           "batch jobs H2D")))
         return st;
@@ -340,11 +340,6 @@ int pbrtgpu_batch_create(const PbrtBatchLimits* limits, PbrtBatch** out) {
         (st = cuda_status(cudaEventCreate(&b->t1), "cudaEventCreate")))
         return fail(st);
     std::memset(b->h, 0, b->lay.pinned);
-    // box filter table (film.rs:89-97): Filter::mean evaluates to 1
-    std::vector<float> table(256, 1.0f);
-    if ((st = cuda_status(cudaMemcpy(b->d + b->lay.table, table.data(), 256 * 4, cudaMemcpyHostToDevice),
-                          "filter table H2D")))
-        return fail(st);
     b->clear();
     *out = b;
     return PBRT_OK;
@@ -384,7 +379,9 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
     const uint32_t cw = P.has_wide ? (uint32_t)wide_stack_variant(P.wide_bound) : 0u;
     const uint32_t j = b->n_jobs;
     const Layout& Y = b->lay;
-    P.filter_table = b->dev<float>(Y.table);
+    float* table = reinterpret_cast<float*>(b->h + Y.o_tables) + (size_t)j * 256;
+    filter_table(*cam, table);  // kind checked by prepare_render
+    P.filter_table = reinterpret_cast<const float*>(b->d + Y.upload + Y.o_tables) + (size_t)j * 256;
     P.tasks = reinterpret_cast<const TaskRec*>(b->d + Y.upload + Y.o_tasks) + b->n_tasks;
     P.n_tasks = smp->num_tasks;
     P.rays = b->dev<PbrtRay>(Y.rays) + b->n_smp;

@@ -126,7 +126,7 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     gather_offsets(cam->filter_x_width, P.sx0, P.sx1, &P.gx0, &P.gx1);
     gather_offsets(cam->filter_y_width, P.sy0, P.sy1, &P.gy0, &P.gy1);
 
-    // task table and box filter table on the host stack (no heap use)
+    // task table and filter table on the host stack (no heap use)
     TaskRec tasks[kNoAllocMaxTasks];
     const float aspect = (float)cam->x_res / (float)cam->y_res;
     const float* crop = cam->crop_window;
@@ -153,7 +153,7 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
         T.fy1 = std::min(te[3], P.fy1);
     }
     float table[256];
-    for (float& v : table) v = 1.0f;
+    if (filter_table(*cam, table)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown filter kind");
 
     const uint64_t S_ = P.n_samples, SL = P.n_samples * (uint64_t)nl;
     const uint64_t npx = (uint64_t)(P.fx1 - P.fx0) * (uint64_t)(P.fy1 - P.fy0);

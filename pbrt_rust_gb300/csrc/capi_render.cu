@@ -308,6 +308,12 @@ int pbrtgpu_scene_bvh(const PbrtScene* S, const PbrtBVH** out) {
     return PBRT_OK;
 }
 
+int pbrtgpu_filter_table(const PbrtCameraDesc* cam, float table[256]) {
+    if (!cam || !table) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (filter_table(*cam, table)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown filter kind");
+    return PBRT_OK;
+}
+
 int pbrtgpu_film_pixel_extent(const PbrtCameraDesc* c, int32_t ext[4]) {
     if (!c || !ext) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     film_extent(c->x_res, c->y_res, c->crop_window, ext);
@@ -342,6 +348,8 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
     if (!(cam->filter_x_width > 0.0f) || !(cam->filter_y_width > 0.0f) || cam->filter_x_width > 16.0f ||
         cam->filter_y_width > 16.0f)
         return set_error(PBRT_ERR_INVALID_ARGUMENT, "filter width must be in (0, 16]");
+    if (cam->filter_kind < PBRT_FILTER_BOX || cam->filter_kind > PBRT_FILTER_LANCZOS)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown filter kind");
     int st;
     if (!S->uploaded && (st = scene_upload(S))) return st;
     const uint32_t nl = (uint32_t)S->lights.size();
@@ -438,8 +446,8 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
     std::lock_guard<std::mutex> lk(S->mu);
     cudaStream_t s = (cudaStream_t)stream_v;
     const uint32_t nl = P.n_lights;
-    // box filter table (film.rs:89-97): Filter::mean evaluates to 1
-    std::vector<float> table(256, 1.0f);
+    std::vector<float> table(256);
+    filter_table(*cam, table.data());  // kind checked by prepare_render
 
     const uint64_t S_ = P.n_samples, SL = P.n_samples * (uint64_t)nl;
     const uint64_t npx = (uint64_t)(P.fx1 - P.fx0) * (uint64_t)(P.fy1 - P.fy0);

@@ -625,3 +625,74 @@ void camera_matrices(const PbrtCameraDesc& cam, float r2c_out[16], float c2w_out
 }
 
 }  // namespace pbrt
+
+namespace pbrt {
+
+// ------------------------------------------------------------------ filter ---
+namespace {
+
+// utils/mod.rs:207-217
+float sinc_1d(float x, float tau) {
+    float v = std::fabs(x);
+    if (v < 1e-5f) return 1.0f;
+    if (v >= 1.0f) return 0.0f;
+    v *= 3.14159265358979323846f;
+    const float vt = v * tau;
+    const float s = std::sin(vt) / vt;
+    return s * std::sin(v) / v;
+}
+
+// filter.rs:87-124 (Filter::evaluate) for the kinds of PBRT_FILTER_*
+float filter_eval(int kind, float xw, float yw, float p0, float p1, float x, float y) {
+    const float ixw = 1.0f / xw, iyw = 1.0f / yw;
+    switch (kind) {
+        case PBRT_FILTER_TRIANGLE: {
+            const float dx = (xw - std::fabs(x)) * ixw, dy = (yw - std::fabs(y)) * iyw;
+            return std::fmax(dx, 0.0f) * std::fmax(dy, 0.0f);
+        }
+        case PBRT_FILTER_GAUSSIAN: {  // filter.rs:55-64: exp_x / exp_y fixed at construction
+            const float ex = std::exp(-p0 * xw * xw), ey = std::exp(-p0 * yw * yw);
+            const float gx = std::fmax(std::exp(-p0 * x * x) - ex, 0.0f);
+            const float gy = std::fmax(std::exp(-p0 * y * y) - ey, 0.0f);
+            return gx * gy;
+        }
+        case PBRT_FILTER_MITCHELL: {
+            const float b = p0, c = p1;
+            auto m = [&](float v) {
+                const float t = std::fabs(v * 2.0f);
+                float r;
+                if (t >= 2.0f)
+                    r = 0.0f;
+                else if (t > 1.0f)
+                    r = (-b - 6.0f * c) * t * t * t + (6.0f * b + 30.0f * c) * t * t + (-12.0f * b - 48.0f * c) * t +
+                        (8.0f * b + 24.0f * c);
+                else
+                    r = (12.0f - 9.0f * b - 6.0f * c) * t * t * t + (-18.0f + 12.0f * b + 6.0f * c) * t * t +
+                        (6.0f - 2.0f * b);
+                return (1.0f / 6.0f) * r;
+            };
+            return m(x * ixw) * m(y * iyw);
+        }
+        case PBRT_FILTER_LANCZOS:
+            return sinc_1d(x * ixw, p0) * sinc_1d(y * iyw, p0);
+        default:  // PBRT_FILTER_BOX: Filter::mean
+            return 1.0f;
+    }
+}
+
+}  // namespace
+
+int filter_table(const PbrtCameraDesc& cam, float table[256]) {
+    if (cam.filter_kind < PBRT_FILTER_BOX || cam.filter_kind > PBRT_FILTER_LANCZOS) return PBRT_ERR_INVALID_ARGUMENT;
+    const float xw = cam.filter_x_width, yw = cam.filter_y_width;
+    for (int y = 0; y < 16; ++y) {
+        const float fy = ((float)y + 0.5f) * yw / 16.0f;
+        for (int x = 0; x < 16; ++x) {
+            const float fx = ((float)x + 0.5f) * xw / 16.0f;
+            table[y * 16 + x] = filter_eval(cam.filter_kind, xw, yw, cam.filter_p0, cam.filter_p1, fx, fy);
+        }
+    }
+    return PBRT_OK;
+}
+
+}  // namespace pbrt

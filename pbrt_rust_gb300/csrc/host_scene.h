@@ -106,4 +106,8 @@ int parse_split_method(const char* s);
 // raster-to-camera and camera-to-world matrices, row-major.
 void camera_matrices(const PbrtCameraDesc& cam, float raster_to_camera[16], float camera_to_world[16]);
 
+// The film's filter table (camera/film.rs:89-97, filter.rs:44-124); returns
+// PBRT_ERR_INVALID_ARGUMENT for an unknown filter kind.
+int filter_table(const PbrtCameraDesc& cam, float table[256]);
+
 }  // namespace pbrt

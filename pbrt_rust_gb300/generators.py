@@ -288,3 +288,32 @@ def orbit_camera(camera, radius: float, azimuth: float, height: float | None = N
     cam2world = Transform.look_at(eye, tuple(target), (0.0, 1.0, 0.0)).inverse()
     return Camera.perspective(cam2world, camera.screen_window, camera.shutter_open, camera.shutter_close,
                               camera.lens_radius, camera.focal_distance, camera.fov, camera.film)
+
+
+def serving_requests(n: int, n_scenes: int, seed: int | None = None, render_fraction: float = 0.5):
+    """The request stream of the serving workload: each request is a render
+    (scene uniform, camera orbiting the scene's centre at radius U[4, 8] with
+    a uniform azimuth, resolution from {128, 256, 512} squared, 1 or 4 spp)
+    or a ray batch of 2^14..2^18 rays with origins in the scene bounds and
+    uniform directions.  Returns dicts describing them; arrival times come
+    from poisson_arrivals."""
+    rng = PCG32(config_seed(4) if seed is None else seed)
+    u = rng.uniform(6 * n).reshape(n, 6)
+    out = []
+    for k in range(n):
+        scene = min(int(u[k, 0] * n_scenes), n_scenes - 1)
+        if u[k, 1] < render_fraction:
+            out.append({"kind": "render", "scene": scene, "res": (128, 256, 512)[min(int(u[k, 2] * 3), 2)],
+                        "spp": (1, 4)[min(int(u[k, 3] * 2), 1)], "radius": 4.0 + 4.0 * u[k, 4],
+                        "azimuth": 2.0 * math.pi * u[k, 5]})
+        else:
+            out.append({"kind": "query", "scene": scene, "n": 1 << (14 + min(int(u[k, 2] * 5), 4)),
+                        "seed": config_seed(4, 1000 + k)})
+    return out
+
+
+def poisson_arrivals(n: int, rate: float, seed: int = 0) -> np.ndarray:
+    """Arrival times (seconds from 0) of a Poisson process of `rate` per
+    second: cumulative sums of exponential gaps drawn by inversion."""
+    u = PCG32(seed).uniform(n)
+    return np.cumsum(-np.log1p(-u) / rate)

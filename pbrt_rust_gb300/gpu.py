@@ -232,4 +232,31 @@ class GpuSamplerRenderer:
             st = self._lib.pbrtgpu_render_tasks(scene._h, C.byref(self._cam), C.byref(self._smp), int(tasks[0]),
                                                 int(tasks[1]), ptr, _stream_handle(stream))
         abi.check(st, self._lib)
+        if self.camera.film.filename and tasks is None:  # sampler_renderer.rs:181: write_image at the end
+            write_image(out, self.camera.film.filename)
         return out
+
+
+def write_image(rgb, path: str) -> None:
+    """Film::write_image (src/camera/film.rs:316-354, write_img :15-33):
+    .png / .ppm with write_img's 8-bit values, .pfm with the linear floats;
+    `rgb` is an (h, w, 3) float32 host array or CUDA tensor."""
+    if _is_torch(rgb):
+        rgb = rgb.detach().cpu().numpy()
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("rgb must have shape (height, width, 3)")
+    lib = abi.load()
+    abi.check(lib.pbrtgpu_write_image(C.c_void_p(a.ctypes.data), a.shape[1], a.shape[0], str(path).encode()), lib)
+
+
+def image_bytes(rgb) -> np.ndarray:
+    """The 8-bit values write_img stores for `rgb` (film.rs:22-24)."""
+    if _is_torch(rgb):
+        rgb = rgb.detach().cpu().numpy()
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    out = np.empty(a.shape, np.uint8)
+    lib = abi.load()
+    abi.check(lib.pbrtgpu_image_bytes(C.c_void_p(a.ctypes.data), a.shape[1], a.shape[0],
+                                      C.c_void_p(out.ctypes.data)), lib)
+    return out

@@ -184,14 +184,34 @@ class SceneDescription:
 # ---------------------------------------------------------- camera & film --
 @dataclass
 class Filter:
-    """Filter::mean (src/filter.rs:45-50): the device film supports the box
-    filter."""
+    """The film's reconstruction filter (src/filter.rs:44-85): ``kind`` is a
+    key of abi.FILTERS; p0 = alpha (gaussian), B (mitchell) or tau
+    (lanczos), p1 = C (mitchell)."""
     x_width: float = 0.5
     y_width: float = 0.5
+    kind: str = "box"
+    p0: float = 0.0
+    p1: float = 0.0
 
     @staticmethod
     def mean(xw: float, yw: float) -> "Filter":
         return Filter(float(xw), float(yw))
+
+    @staticmethod
+    def triangle(xw: float, yw: float) -> "Filter":
+        return Filter(float(xw), float(yw), "triangle")
+
+    @staticmethod
+    def gaussian(xw: float, yw: float, a: float) -> "Filter":
+        return Filter(float(xw), float(yw), "gaussian", float(a))
+
+    @staticmethod
+    def mitchell(xw: float, yw: float, b: float, c: float) -> "Filter":
+        return Filter(float(xw), float(yw), "mitchell", float(b), float(c))
+
+    @staticmethod
+    def lanczos(xw: float, yw: float, tau: float) -> "Filter":
+        return Filter(float(xw), float(yw), "lanczos", float(tau))
 
 
 @dataclass
@@ -253,6 +273,9 @@ class Camera:
         d.crop_window[:] = list(self.film.crop)
         d.filter_x_width = self.film.filter.x_width
         d.filter_y_width = self.film.filter.y_width
+        d.filter_kind = abi.FILTERS[self.film.filter.kind]
+        d.filter_p0 = self.film.filter.p0
+        d.filter_p1 = self.film.filter.p1
         return d
 
 

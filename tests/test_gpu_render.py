@@ -106,3 +106,23 @@ def test_task_shards_sum_to_the_frame():
         assert np.array_equal(acc.view(np.uint32), full.view(np.uint32))
     empty = r.render(scene, tasks=(2, 2))
     assert not empty.any()
+
+
+@pytest.mark.parametrize("filt", [Filter.triangle(2.0, 1.5), Filter.gaussian(2.0, 2.0, 2.0),
+                                  Filter.mitchell(2.0, 2.0, 1.0 / 3.0, 1.0 / 3.0), Filter.lanczos(3.0, 2.5, 3.0)],
+                         ids=lambda f: f.kind)
+def test_filters_match_oracle(oracle, filt):
+    """Wide, negative-lobed and separable filters: every pixel gathers the
+    samples of its neighbours with the table weights."""
+    prims, lights, cam, _ = G.c1_scene(res=56)
+    cam = Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, cam.fov,
+                             Film.image(56, 40, filt))
+    smp = StratifiedSampler.stratified(0, 56, 0, 40, 2, 2, True, 0.0, 1.0)
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert_image_close(gpu, ref)
+    prims, lights, cam, _ = G.c1_scene(res=48, n_spheres=0)
+    cam = Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, cam.fov,
+                             Film.image(48, 48, filt))
+    smp = StratifiedSampler.stratified(0, 48, 0, 48, 2, 2, True, 0.0, 1.0)
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
