@@ -81,6 +81,34 @@ def mat_inverse(a: np.ndarray) -> np.ndarray:
     return inv
 
 
+_libm = None
+
+
+def _libm_f(name: str):
+    """The C library's f32 function (what Rust's f32 methods call on Linux)."""
+    global _libm
+    import ctypes
+    import ctypes.util
+    if _libm is None:
+        _libm = ctypes.CDLL(ctypes.util.find_library("m") or None)
+    fn = getattr(_libm, name)
+    fn.restype, fn.argtypes = ctypes.c_float, [ctypes.c_float]
+    return fn
+
+
+def _sinf(x) -> np.float32:
+    return F(_libm_f("sinf")(float(x)))
+
+
+def _cosf(x) -> np.float32:
+    return F(_libm_f("cosf")(float(x)))
+
+
+def _as_radians(deg) -> np.float32:
+    """utils/mod.rs: degrees * pi / 180 in f32."""
+    return F(F(F(deg) * F(np.pi)) / F(180.0))
+
+
 def _v(x) -> tuple:
     return tuple(F(c) for c in x)
 
@@ -140,6 +168,26 @@ class Transform:
         m[0, 1], m[1, 1], m[2, 1], m[3, 1] = new_up[0], new_up[1], new_up[2], ZERO
         m[0, 2], m[1, 2], m[2, 2], m[3, 2] = d[0], d[1], d[2], ZERO
         return Transform(mat_inverse(m), m)
+
+    @staticmethod
+    def rotate(angle, axis) -> "Transform":
+        """transform.rs:117-142 (the inverse is the transpose)."""
+        a = _normalize(_v(axis))
+        th = _as_radians(angle)
+        s, c = _sinf(th), _cosf(th)
+        ax, ay, az = a
+        one_c = F(ONE - c)
+        m = identity()
+        m[0, 0] = F(ax * ax + F(F(ONE - F(ax * ax)) * c))
+        m[0, 1] = F(F(F(ax * ay) * one_c) - F(az * s))
+        m[0, 2] = F(F(F(ax * az) * one_c) + F(ay * s))
+        m[1, 0] = F(F(F(ax * ay) * one_c) + F(az * s))
+        m[1, 1] = F(ay * ay + F(F(ONE - F(ay * ay)) * c))
+        m[1, 2] = F(F(F(ay * az) * one_c) - F(ax * s))
+        m[2, 0] = F(F(F(ax * az) * one_c) - F(ay * s))
+        m[2, 1] = F(F(F(ay * az) * one_c) + F(ax * s))
+        m[2, 2] = F(az * az + F(F(ONE - F(az * az)) * c))
+        return Transform(m, m.T.copy())
 
     def inverse(self) -> "Transform":
         return Transform(self.m_inv, self.m)

@@ -126,3 +126,22 @@ def test_filters_match_oracle(oracle, filt):
     smp = StratifiedSampler.stratified(0, 48, 0, 48, 2, 2, True, 0.0, 1.0)
     gpu, ref = render_both(oracle, prims, lights, cam, smp)
     assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
+
+
+def test_scene_file_renders_on_the_device(oracle, tmp_path):
+    """A pbrt-v2 scene file through the API (pbrt_rust_gb300.api) renders on
+    the device as the oracle renders the parsed scene, and its film file is
+    written."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from test_api import SCENE
+
+    from pbrt_rust_gb300 import api as A
+    text = SCENE.replace('Film "image"', f'Film "image" "string filename" "{tmp_path / "out.png"}"')
+    frame = A.parse(text).frames[0]
+    gpu = frame.render()
+    ref = oracle.render(SceneDescription(frame.primitives, frame.lights, frame.max_prims, frame.split_method),
+                        frame.camera, frame.sampler, frame.num_tasks)
+    assert_image_close(gpu, ref)
+    assert (tmp_path / "out.png").stat().st_size > 40 * 32 * 3
