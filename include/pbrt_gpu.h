@@ -67,7 +67,7 @@ typedef struct PbrtTransform {
     float m_inv[16];
 } PbrtTransform;
 
-enum { PBRT_SHAPE_TRIANGLE_MESH = 0, PBRT_SHAPE_SPHERE = 1 };
+enum { PBRT_SHAPE_TRIANGLE_MESH = 0, PBRT_SHAPE_SPHERE = 1, PBRT_SHAPE_DISK = 2, PBRT_SHAPE_CYLINDER = 3 };
 enum { PBRT_SPLIT_SAH = 0, PBRT_SPLIT_MIDDLE = 1, PBRT_SPLIT_EQUAL = 2 };
 
 /* One input primitive.  Mirrors Shape::triangle_mesh and Shape::sphere
@@ -84,8 +84,12 @@ typedef struct PbrtShapeDesc {
     uint32_t n_points;
     const uint32_t* indices;      /* n_indices, a multiple of 3 */
     uint32_t n_indices;
-    /* sphere (src/shape/sphere.rs:28-44) */
+    /* sphere (src/shape/sphere.rs:28-44): radius, z0, z1, phi_max_deg;
+     * cylinder (src/shape/cylinder.rs:26-36): radius, z0, z1, phi_max_deg;
+     * disk (src/shape/disk.rs:24-34): height, radius, inner_radius,
+     * phi_max_deg */
     float radius, z0, z1, phi_max_deg;
+    float height, inner_radius;
     /* render-only */
     int32_t material;             /* index into PbrtSceneDesc.materials */
     int32_t area_light;           /* index into PbrtSceneDesc.lights or -1 */

@@ -613,10 +613,15 @@ void tri_dg(const Tri& tr, const Ray& r, float t, V3* p, V3* nn, V3* dpdu_out) {
     if (dpdu_out) *dpdu_out = dpdu;
 }
 
+// Analytic shapes: sphere (sphere.rs:16-25), disk (disk.rs:16-22) and
+// cylinder (cylinder.rs:16-23).  A disk keeps its height in z_min = z_max.
+enum { QUAD_SPHERE = 0, QUAD_DISK = 1, QUAD_CYLINDER = 2 };
 struct Sphere {
     Xf o2w, w2o;
     bool flip;
     float radius, phi_max, z_min, z_max, theta_min, theta_max;
+    int kind = QUAD_SPHERE;
+    float height = 0.0f, inner_radius = 0.0f;
 };
 // sphere.rs:28-44
 Sphere sphere_new(const Xf& o2w, const Xf& w2o, bool ro, float rad, float z0, float z1, float pm) {
@@ -632,7 +637,34 @@ Sphere sphere_new(const Xf& o2w, const Xf& w2o, bool ro, float rad, float z0, fl
     s.phi_max = as_radians(clampf(pm, 0.0f, 360.0f));
     return s;
 }
-// sphere.rs:111-126
+// disk.rs:24-34
+Sphere disk_new(const Xf& o2w, const Xf& w2o, bool ro, float ht, float r, float ri, float tmax) {
+    Sphere s{};
+    s.o2w = o2w;
+    s.w2o = w2o;
+    s.flip = ro != swaps_handedness(o2w.m);
+    s.kind = QUAD_DISK;
+    s.height = ht;
+    s.radius = r;
+    s.inner_radius = ri;
+    s.z_min = s.z_max = ht;
+    s.phi_max = as_radians(clampf(tmax, 0.0f, 360.0f));
+    return s;
+}
+// cylinder.rs:26-36
+Sphere cylinder_new(const Xf& o2w, const Xf& w2o, bool ro, float rad, float z0, float z1, float pm) {
+    Sphere s{};
+    s.o2w = o2w;
+    s.w2o = w2o;
+    s.flip = ro != swaps_handedness(o2w.m);
+    s.kind = QUAD_CYLINDER;
+    s.radius = rad;
+    s.z_min = fminf(z0, z1);
+    s.z_max = fmaxf(z0, z1);
+    s.phi_max = as_radians(clampf(pm, 0.0f, 360.0f));
+    return s;
+}
+// sphere.rs:111-126, disk.rs:68-74, cylinder.rs:96-100
 BBox sphere_bound(const Sphere& s) {
     BBox ob{mk(-s.radius, -s.radius, s.z_min), mk(s.radius, s.radius, s.z_max)};
     return xf_bbox(s.o2w.m, ob);
@@ -682,6 +714,101 @@ bool sphere_hit_obj(const Sphere& s, const Ray& ray, float* t_out, float* phi_ou
     *t_out = t_hit;
     *phi_out = phi;
     return true;
+}
+// disk.rs:36-66 (ray in object space)
+bool disk_hit_obj(const Sphere& s, const Ray& ray, float* t_out, float* phi_out) {
+    if (fabsf(ray.d.z) < 1e-6f) return false;
+    float t_hit = (s.height - ray.o.z) / ray.d.z;
+    if (t_hit < ray.mint || t_hit > ray.maxt) return false;
+    V3 p = point_at(ray, t_hit);
+    float dist2 = p.x * p.x + p.y * p.y;
+    if (dist2 > (s.radius * s.radius) || dist2 < (s.inner_radius * s.inner_radius)) return false;
+    float phi = atan2f(p.y, p.x);
+    if (phi < 0.0f) phi = phi + 2.0f * kPi;
+    if (phi > s.phi_max) return false;
+    *t_out = t_hit;
+    *phi_out = phi;
+    return true;
+}
+// cylinder.rs:38-94 (ray in object space)
+bool cylinder_hit_obj(const Sphere& s, const Ray& ray, float* t_out, float* phi_out) {
+    float a = ray.d.x * ray.d.x + ray.d.y * ray.d.y;
+    float b = 2.0f * (ray.d.x * ray.o.x + ray.d.y * ray.o.y);
+    float c = ray.o.x * ray.o.x + ray.o.y * ray.o.y - s.radius * s.radius;
+    float t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0 > ray.maxt || t1 < ray.mint) return false;
+    float t_hit = t0;
+    if (t0 < ray.mint) {
+        t_hit = t1;
+        if (t_hit > ray.maxt) return false;
+    }
+    auto get_hit = [&](float t, V3* hit, float* angle) {
+        V3 h = point_at(ray, t);
+        if (h.x == 0.0f && h.y == 0.0f) h.x = 1e-5f * s.radius;
+        float a2 = atan2f(h.y, h.x);
+        if (a2 < 0.0f) a2 = a2 + 2.0f * kPi;
+        *hit = h;
+        *angle = a2;
+    };
+    auto invalid = [&](V3 h, float phi) { return h.z < s.z_min || h.z > s.z_max || phi > s.phi_max; };
+    V3 h;
+    float phi;
+    get_hit(t_hit, &h, &phi);
+    if (invalid(h, phi)) {
+        if (t_hit == t1) return false;
+        if (t1 > ray.maxt) return false;
+        t_hit = t1;
+        get_hit(t_hit, &h, &phi);
+        if (invalid(h, phi)) return false;
+    }
+    *t_out = t_hit;
+    *phi_out = phi;
+    return true;
+}
+bool quad_hit_obj(const Sphere& s, const Ray& ray, float* t_out, float* phi_out) {
+    if (s.kind == QUAD_DISK) return disk_hit_obj(s, ray, t_out, phi_out);
+    if (s.kind == QUAD_CYLINDER) return cylinder_hit_obj(s, ray, t_out, phi_out);
+    return sphere_hit_obj(s, ray, t_out, phi_out);
+}
+// transform.rs:220-227: normals go through the inverse transpose
+V3 xf_normal(const M4& m_inv, V3 n) {
+    return mk(m_inv.m[0][0] * n.x + m_inv.m[1][0] * n.y + m_inv.m[2][0] * n.z,
+              m_inv.m[0][1] * n.x + m_inv.m[1][1] * n.y + m_inv.m[2][1] * n.z,
+              m_inv.m[0][2] * n.x + m_inv.m[1][2] * n.y + m_inv.m[2][2] * n.z);
+}
+// disk.rs:96-131 and cylinder.rs:131-166 (with helpers.rs:17-43): hit point
+// and geometric normal.  The disk's normal is the transformed +-z by the side
+// of the object-space ray origin, not normalised nor flipped.
+void quad_dg(const Sphere& s, const Ray& obj_ray, float t_hit, float phi, V3* p, V3* nn, float* u_out,
+             float* v_out, V3* dpdu_o, V3* dpdv_o) {
+    V3 ph = point_at(obj_ray, t_hit);
+    *p = xf_point(s.o2w.m, ph);
+    if (s.kind == QUAD_DISK) {
+        float dist = sqrtf(ph.x * ph.x + ph.y * ph.y);
+        float u = phi / s.phi_max;
+        float v = 1.0f - (dist - s.inner_radius) / (s.radius - s.inner_radius);
+        V3 dpdu = mul(mk(-s.phi_max * ph.y, s.phi_max * ph.x, 0.0f), s.phi_max / (2.0f * kPi));
+        V3 dpdv = mul(mk(ph.x, ph.y, 0.0f), (s.inner_radius - s.radius) / dist);
+        *nn = xf_normal(s.w2o.m, mk(0.0f, 0.0f, obj_ray.o.z > 0.0f ? 1.0f : -1.0f));
+        if (u_out) *u_out = u;
+        if (v_out) *v_out = v;
+        if (dpdu_o) *dpdu_o = xf_vector(s.o2w.m, dpdu);
+        if (dpdv_o) *dpdv_o = xf_vector(s.o2w.m, dpdv);
+        return;
+    }
+    float u = phi / s.phi_max;
+    float v = (ph.z - s.z_min) / (s.z_max - s.z_min);
+    V3 dpdu = mul(mk(-ph.y, ph.x, 0.0f), s.phi_max);
+    V3 dpdv = mk(0.0f, 0.0f, s.z_max - s.z_min);
+    V3 du = xf_vector(s.o2w.m, dpdu), dv = xf_vector(s.o2w.m, dpdv);
+    V3 n = normalize(cross(du, dv));
+    if (s.flip) n = mul(n, -1.0f);
+    *nn = n;
+    if (u_out) *u_out = u;
+    if (v_out) *v_out = v;
+    if (dpdu_o) *dpdu_o = du;
+    if (dpdv_o) *dpdv_o = dv;
 }
 // sphere.rs:135-176 + shape/helpers.rs:17-43 + diff_geom.rs:52-79
 void sphere_dg(const Sphere& s, const Ray& obj_ray, float t_hit, float phi, V3* p, V3* nn, V3* dpdu_w,
@@ -760,9 +887,13 @@ bool refine_shapes(const PbrtShapeDesc* shapes, uint32_t n, Refined* out) {
                 p.sphere = -1;
                 out->prims.push_back(p);
             }
-        } else if (d.kind == PBRT_SHAPE_SPHERE) {
-            Sphere s = sphere_new(o2w, xf_inverse(o2w), d.reverse_orientation != 0, d.radius, d.z0, d.z1,
-                                  d.phi_max_deg);
+        } else if (d.kind == PBRT_SHAPE_SPHERE || d.kind == PBRT_SHAPE_DISK || d.kind == PBRT_SHAPE_CYLINDER) {
+            const bool ro = d.reverse_orientation != 0;
+            Sphere s = d.kind == PBRT_SHAPE_SPHERE
+                           ? sphere_new(o2w, xf_inverse(o2w), ro, d.radius, d.z0, d.z1, d.phi_max_deg)
+                       : d.kind == PBRT_SHAPE_DISK
+                           ? disk_new(o2w, xf_inverse(o2w), ro, d.height, d.radius, d.inner_radius, d.phi_max_deg)
+                           : cylinder_new(o2w, xf_inverse(o2w), ro, d.radius, d.z0, d.z1, d.phi_max_deg);
             Prim p;
             p.kind = KIND_SPHERE;
             p.shape = (int)si;
@@ -1034,7 +1165,7 @@ bool prim_intersect(const Refined& R, const Prim& p, Ray& ray, float* t, float* 
         const Sphere& s = R.spheres[p.sphere];
         Ray oray = xf_ray(s.w2o.m, ray);
         float phi;
-        if (!sphere_hit_obj(s, oray, t, &phi)) return false;
+        if (!quad_hit_obj(s, oray, t, &phi)) return false;
         *b1 = 0.0f;
         *b2 = 0.0f;
     }
@@ -1426,8 +1557,11 @@ bool scene_intersect(const SceneData& S, const Ray& r_in, SurfHit* sh, Counters&
         Ray orr = xf_ray(s.w2o.m, r_in);
         orr.maxt = r_in.maxt;
         float t, phi;
-        sphere_hit_obj(s, orr, &t, &phi);  // recompute phi for u (same t)
-        sphere_dg(s, orr, h.t, phi, &sh->p, &sh->nn, nullptr, nullptr, nullptr, nullptr, nullptr);
+        quad_hit_obj(s, orr, &t, &phi);  // recompute phi for u (same t)
+        if (s.kind == QUAD_SPHERE)
+            sphere_dg(s, orr, h.t, phi, &sh->p, &sh->nn, nullptr, nullptr, nullptr, nullptr, nullptr);
+        else
+            quad_dg(s, orr, h.t, phi, &sh->p, &sh->nn, nullptr, nullptr, nullptr, nullptr);
     }
     return true;
 }
@@ -1837,6 +1971,26 @@ int oracle_sphere_intersect(const PbrtTransform* o2w, float radius, float z0, fl
         V3 p, nn, du, dv;
         float u, v;
         sphere_dg(s, orr, t, phi, &p, &nn, nullptr, &u, &v, &du, &dv);
+        float o[16] = {t, t * 5e-4f, p.x, p.y, p.z, nn.x, nn.y, nn.z, u, v, du.x, du.y, du.z, dv.x, dv.y, dv.z};
+        memcpy(out, o, sizeof(o));
+    } else if (out) {
+        out[0] = t;
+    }
+    return 1;
+}
+int oracle_quadric_intersect(int kind, const PbrtTransform* o2w, float a, float b, float c, float phimax,
+                             const PbrtRay* ray, int mode, float out[16]) {
+    Xf x = xf_from_desc(*o2w);
+    Sphere s = kind == PBRT_SHAPE_DISK ? disk_new(x, xf_inverse(x), false, a, b, c, phimax)
+                                       : cylinder_new(x, xf_inverse(x), false, a, b, c, phimax);
+    Ray r = to_ray(*ray);
+    Ray orr = xf_ray(s.w2o.m, r);
+    float t, phi;
+    if (!quad_hit_obj(s, orr, &t, &phi)) return 0;
+    if (mode == 1) {
+        V3 p, nn, du, dv;
+        float u, v;
+        quad_dg(s, orr, t, phi, &p, &nn, &u, &v, &du, &dv);
         float o[16] = {t, t * 5e-4f, p.x, p.y, p.z, nn.x, nn.y, nn.z, u, v, du.x, du.y, du.z, dv.x, dv.y, dv.z};
         memcpy(out, o, sizeof(o));
     } else if (out) {

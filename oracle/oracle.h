@@ -89,6 +89,11 @@ int oracle_triangle_intersect(const float tri[9], const PbrtRay* ray, float out[
 /* Sphere (o2w transform, radius, z0, z1, phimax degrees):
  * mode 0 = intersect_p; mode 1 = intersect with dg.
  * out (mode 1): t, eps, p.xyz, nn.xyz, u, v, dpdu.xyz, dpdv.xyz (16 floats). */
+/* Disk (kind PBRT_SHAPE_DISK: a = height, b = radius, c = inner radius) or
+ * cylinder (PBRT_SHAPE_CYLINDER: a = radius, b = z0, c = z1) against a ray;
+ * out as oracle_sphere_intersect. */
+int oracle_quadric_intersect(int kind, const PbrtTransform* o2w, float a, float b, float c, float phimax,
+                             const PbrtRay* ray, int mode, float out[16]);
 int oracle_sphere_intersect(const PbrtTransform* o2w, float radius, float z0, float z1,
                             float phimax, const PbrtRay* ray, int mode, float out[16]);
 int oracle_matrix_invert(const float m[16], float out[16]);

@@ -57,6 +57,8 @@ def load() -> C.CDLL:
             "oracle_bbox_intersect": (C.c_int, [_P, _P, _P, _P]),
             "oracle_bbox_metrics": (None, [_P, _P, _P, _P]),
             "oracle_triangle_intersect": (C.c_int, [_P, _P, _P]),
+            "oracle_quadric_intersect": (C.c_int, [C.c_int, C.POINTER(abi.PbrtTransform), C.c_float, C.c_float,
+                                                   C.c_float, C.c_float, _P, C.c_int, _P]),
             "oracle_sphere_intersect": (C.c_int, [C.POINTER(abi.PbrtTransform), C.c_float, C.c_float, C.c_float,
                                                   C.c_float, _P, C.c_int, _P]),
             "oracle_matrix_invert": (C.c_int, [_P, _P]),

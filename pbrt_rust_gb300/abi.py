@@ -23,6 +23,8 @@ STATUS_NAMES = {
 
 SHAPE_TRIANGLE_MESH = 0
 SHAPE_SPHERE = 1
+SHAPE_DISK = 2
+SHAPE_CYLINDER = 3
 LIGHT_POINT = 0
 LIGHT_DIFFUSE_AREA = 1
 SPLIT_METHODS = {"sah": 0, "middle": 1, "equal": 2}
@@ -51,6 +53,7 @@ class PbrtShapeDesc(C.Structure):
         ("points", C.POINTER(C.c_float)), ("n_points", C.c_uint32),
         ("indices", C.POINTER(C.c_uint32)), ("n_indices", C.c_uint32),
         ("radius", C.c_float), ("z0", C.c_float), ("z1", C.c_float), ("phi_max_deg", C.c_float),
+        ("height", C.c_float), ("inner_radius", C.c_float),
         ("material", C.c_int32), ("area_light", C.c_int32),
     ]
 

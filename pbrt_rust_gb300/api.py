@@ -20,12 +20,13 @@ direct-lighting Li), Accelerator "bvh" (maxnodeprims, splitmethod),
 WorldBegin/WorldEnd, AttributeBegin/End, TransformBegin/End,
 ReverseOrientation, Material / MakeNamedMaterial / NamedMaterial "matte",
 Texture "constant", LightSource "point", AreaLightSource "diffuse" on
-triangle meshes, Shape "sphere" and "trianglemesh", ObjectBegin/End and
+triangle meshes, Shape "sphere", "disk", "cylinder" and "trianglemesh", ObjectBegin/End and
 ObjectInstance (flattened into the scene, see ``object_instance``), Include.
 Anything else raises ``NotImplementedError`` (the reference panics).
 """
 from __future__ import annotations
 
+import dataclasses
 import os
 import re
 from dataclasses import dataclass, field
@@ -173,6 +174,12 @@ def make_shape(name: str, o2w: Transform, w2o: Transform, ro: bool, ps: ParamSet
         zmax = ps.find_one_float("zmax", radius)
         phimax = ps.find_one_float("phimax", 360.0)
         return Shape.sphere(o2w, w2o, ro, radius, zmin, zmax, phimax)
+    if name == "disk":  # pbrt-v2 defaults
+        return Shape.disk(o2w, w2o, ro, ps.find_one_float("height", 0.0), ps.find_one_float("radius", 1.0),
+                          ps.find_one_float("innerradius", 0.0), ps.find_one_float("phimax", 360.0))
+    if name == "cylinder":
+        return Shape.cylinder(o2w, w2o, ro, ps.find_one_float("radius", 1.0), ps.find_one_float("zmin", -1.0),
+                              ps.find_one_float("zmax", 1.0), ps.find_one_float("phimax", 360.0))
     if name == "trianglemesh":
         vi = ps.find_int("indices")
         p = ps.find_point("P")
@@ -514,8 +521,7 @@ class Pbrt:
         inst = self.ctm[0]
         for p in self.instances[name]:
             s = p.shape
-            moved = Shape(s.kind, inst * s.object_to_world, s.reverse_orientation, s.points, s.indices, s.radius,
-                          s.z0, s.z1, s.phi_max)
+            moved = dataclasses.replace(s, object_to_world=inst * s.object_to_world)
             if p.area_light is not None:
                 light = DiffuseAreaLight(inst * p.area_light.light_to_world, p.area_light.radiance)
                 q = Primitive.geometric_area_light(moved, p.material, light)

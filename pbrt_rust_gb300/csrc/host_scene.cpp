@@ -576,8 +576,39 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
             // <= 2*pi in f32.
             s.full = (s.z_min <= -rad && s.z_max >= rad && s.phi_max >= 2.0f * 3.14159265358979323846f) ? 1u : 0u;
             s.flip = flip ? 1u : 0u;
+            s.kind = kQuadSphere;
             HostPrim p{};
             p.kind = PBRT_SHAPE_SPHERE;
+            p.shape = (int)si;
+            p.material = d.material;
+            p.area_light = d.area_light;
+            p.flip = flip;
+            p.sphere = (int)H.spheres.size();
+            H.spheres.push_back(s);
+            H.prims.push_back(p);
+            H.has_spheres = true;
+        } else if (d.kind == PBRT_SHAPE_DISK || d.kind == PBRT_SHAPE_CYLINDER) {
+            SphereRec s{};
+            std::memcpy(s.o2w, o2w.m.m, sizeof(s.o2w));
+            std::memcpy(s.w2o, o2w.mi.m, sizeof(s.w2o));
+            s.radius = d.radius;
+            s.phi_max = clampf(d.phi_max_deg, 0.0f, 360.0f) * 3.14159265358979323846f / 180.0f;
+            if (d.kind == PBRT_SHAPE_DISK) {  // disk.rs:24-34: radii unclamped
+                s.kind = kQuadDisk;
+                s.height = d.height;
+                s.inner_radius = d.inner_radius;
+                s.z_min = s.z_max = d.height;
+            } else {  // cylinder.rs:26-36
+                s.kind = kQuadCylinder;
+                s.z_min = std::fmin(d.z0, d.z1);
+                s.z_max = std::fmax(d.z0, d.z1);
+            }
+            // phi = atan2 (+ 2 pi when negative) stays <= 2 pi in f32, so a
+            // full turn never rejects on phi
+            s.full = s.phi_max >= 2.0f * 3.14159265358979323846f ? 1u : 0u;
+            s.flip = flip ? 1u : 0u;
+            HostPrim p{};
+            p.kind = PBRT_SHAPE_SPHERE;  // refined like a sphere: one analytic primitive
             p.shape = (int)si;
             p.material = d.material;
             p.area_light = d.area_light;

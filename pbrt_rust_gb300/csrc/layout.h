@@ -68,14 +68,22 @@ struct alignas(16) PrimRec {
 static_assert(sizeof(PrimRec) == 48, "primitive record is 48 bytes");
 constexpr uint32_t kSphereBit = 0x80000000u;
 
-// Sphere (src/shape/sphere.rs:16-25) with its world-to-object matrix rows.
+// An analytic shape - sphere (src/shape/sphere.rs:16-25), disk
+// (src/shape/disk.rs:16-22) or cylinder (src/shape/cylinder.rs:16-23) -
+// with its world-to-object and object-to-world matrix rows.  A disk keeps
+// its height in z_min = z_max (its object bound, disk.rs:70-74).
+enum { kQuadSphere = 0, kQuadDisk = 1, kQuadCylinder = 2 };
 struct alignas(16) SphereRec {
     float w2o[16];      // row-major world_to_object.m
     float o2w[16];      // row-major object_to_world.m
     float radius, z_min, z_max, phi_max;
     float theta_min, theta_max;
-    uint32_t full;      // no z or phi clipping can apply
+    uint32_t full;      // the phi (and for spheres the z) clip cannot reject
     uint32_t flip;      // reverse_orientation ^ transform_swaps_handedness
+    uint32_t kind;      // kQuad*
+    float height, inner_radius;
+    uint32_t pad;
 };
+static_assert(sizeof(SphereRec) == 176, "analytic shape record is 176 bytes");
 
 }  // namespace pbrt

@@ -192,12 +192,67 @@ __device__ __forceinline__ bool sphere_obj_test(const SphereRec& s, const float*
     return true;
 }
 
+__device__ __forceinline__ float phi_of(float x, float y) {  // atan2, moved to [0, 2 pi)
+    float a = atan2f(y, x);
+    if (a < 0.0f) a += 2.0f * 3.14159265358979323846f;
+    return a;
+}
+
+// src/shape/disk.rs:36-66 on the object-space ray.
+__device__ __forceinline__ bool disk_obj_test(const SphereRec& s, const float* o, const float* d, float mint,
+                                              float maxt, float* t_out) {
+    if (fabsf(d[2]) < 1e-6f) return false;
+    const float t = (s.height - o[2]) / d[2];
+    if (t < mint || t > maxt) return false;
+    const float px = o[0] + d[0] * t, py = o[1] + d[1] * t;
+    const float dist2 = px * px + py * py;
+    if (dist2 > (s.radius * s.radius) || dist2 < (s.inner_radius * s.inner_radius)) return false;
+    if (!s.full && phi_of(px, py) > s.phi_max) return false;
+    *t_out = t;
+    return true;
+}
+
+// src/shape/cylinder.rs:38-94 on the object-space ray; the z clip always
+// applies, the phi clip only to partial cylinders.
+__device__ __forceinline__ bool cylinder_obj_test(const SphereRec& s, const float* o, const float* d, float mint,
+                                                  float maxt, float* t_out) {
+    const float a = d[0] * d[0] + d[1] * d[1];
+    const float b = 2.0f * (d[0] * o[0] + d[1] * o[1]);
+    const float c = o[0] * o[0] + o[1] * o[1] - s.radius * s.radius;
+    float t0, t1;
+    if (!quadratic(a, b, c, &t0, &t1)) return false;
+    if (t0 > maxt || t1 < mint) return false;
+    float th = t0;
+    if (t0 < mint) {
+        th = t1;
+        if (th > maxt) return false;
+    }
+    auto invalid = [&](float t) {
+        float hx = o[0] + d[0] * t, hy = o[1] + d[1] * t, hz = o[2] + d[2] * t;
+        if (hz < s.z_min || hz > s.z_max) return true;
+        if (s.full) return false;
+        if (hx == 0.0f && hy == 0.0f) hx = 1e-5f * s.radius;
+        return phi_of(hx, hy) > s.phi_max;
+    };
+    if (invalid(th)) {
+        if (th == t1) return false;
+        if (t1 > maxt) return false;
+        th = t1;
+        if (invalid(th)) return false;
+    }
+    *t_out = th;
+    return true;
+}
+
+// Any analytic shape (SphereRec::kind) against the world-space ray.
 __device__ __forceinline__ bool sphere_test(const SphereRec* spheres, uint32_t si, const DRay& r, float maxt,
                                             float* t_out) {
     const SphereRec& s = spheres[si];
     float o[3], d[3];
     xf_point(s.w2o, r.ox, r.oy, r.oz, o);
     xf_vector(s.w2o, r.dx, r.dy, r.dz, d);
+    if (s.kind == kQuadDisk) return disk_obj_test(s, o, d, r.tmin, maxt, t_out);
+    if (s.kind == kQuadCylinder) return cylinder_obj_test(s, o, d, r.tmin, maxt, t_out);
     return sphere_obj_test(s, o, d, r.tmin, maxt, t_out);
 }
 

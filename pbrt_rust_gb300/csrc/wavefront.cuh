@@ -277,7 +277,34 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
         float t = h.y;
         const ShadePrim& sp = P.shade[prim];
         uint32_t flags = __float_as_uint(sp.c[3]);
-        if (flags & kShadeSphere) {
+        if ((flags & kShadeSphere) && P.spheres[flags >> 2].kind != kQuadSphere) {
+            const SphereRec& S = P.spheres[flags >> 2];
+            float o[3], d[3];
+            xf_point(S.w2o, r.ox, r.oy, r.oz, o);
+            xf_vector(S.w2o, r.dx, r.dy, r.dz, d);
+            const V ph = mkv(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
+            float pw[3];
+            xf_point(S.o2w, ph.x, ph.y, ph.z, pw);
+            p = ld3(pw);
+            if (S.kind == kQuadDisk) {
+                // disk.rs:106-129: the normal is the transformed +-z (by the
+                // side of the object-space ray origin), neither normalised
+                // nor flipped
+                const float nz = o[2] > 0.0f ? 1.0f : -1.0f;  // transform.rs:220-227 (inverse transpose)
+                nn = mkv(S.w2o[0] * 0.0f + S.w2o[4] * 0.0f + S.w2o[8] * nz,
+                         S.w2o[1] * 0.0f + S.w2o[5] * 0.0f + S.w2o[9] * nz,
+                         S.w2o[2] * 0.0f + S.w2o[6] * 0.0f + S.w2o[10] * nz);
+            } else {
+                // cylinder.rs:143-164 + helpers.rs:17-43 + diff_geom.rs:52-79
+                V dpdu = mkv(S.phi_max * -ph.y, S.phi_max * ph.x, 0.0f);
+                V dpdv = mkv(0.0f, 0.0f, S.z_max - S.z_min);
+                float du[3], dv[3];
+                xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
+                xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
+                nn = vnorm(vcross(ld3(du), ld3(dv)));
+                if (S.flip) nn = vmul(nn, -1.0f);
+            }
+        } else if (flags & kShadeSphere) {
             // sphere.rs:135-176 + shape/helpers.rs:17-43 + diff_geom.rs:52-79
             const SphereRec& S = P.spheres[flags >> 2];
             float o[3], d[3];

@@ -34,6 +34,8 @@ class Shape:
     z0: float = -1.0
     z1: float = 1.0
     phi_max: float = 360.0
+    height: float = 0.0        # disk
+    inner_radius: float = 0.0  # disk
 
     @staticmethod
     def triangle_mesh(o2w: Transform, w2o: Transform | None, ro: bool, vi, p) -> "Shape":
@@ -55,6 +57,20 @@ class Shape:
             raise ValueError("sphere radius must be positive (sphere.rs:30)")
         return Shape(abi.SHAPE_SPHERE, o2w, bool(ro), radius=float(rad), z0=float(z0), z1=float(z1),
                      phi_max=float(pm))
+
+    @staticmethod
+    def disk(o2w: Transform, w2o: Transform | None, ro: bool, height: float, radius: float, inner_radius: float,
+             phi_max: float) -> "Shape":
+        """Disk::new (src/shape/disk.rs:24-34)."""
+        return Shape(abi.SHAPE_DISK, o2w, bool(ro), radius=float(radius), phi_max=float(phi_max),
+                     height=float(height), inner_radius=float(inner_radius))
+
+    @staticmethod
+    def cylinder(o2w: Transform, w2o: Transform | None, ro: bool, radius: float, z0: float, z1: float,
+                 phi_max: float) -> "Shape":
+        """Cylinder::new (src/shape/cylinder.rs:26-36)."""
+        return Shape(abi.SHAPE_CYLINDER, o2w, bool(ro), radius=float(radius), z0=float(z0), z1=float(z1),
+                     phi_max=float(phi_max))
 
     def num_primitives(self) -> int:
         return len(self.indices) // 3 if self.kind == abi.SHAPE_TRIANGLE_MESH else 1
@@ -137,6 +153,7 @@ class SceneDescription:
                 d.indices = abi.u32p(s.indices)
                 d.n_indices = len(s.indices)
             d.radius, d.z0, d.z1, d.phi_max_deg = s.radius, s.z0, s.z1, s.phi_max
+            d.height, d.inner_radius = s.height, s.inner_radius
             d.material = mat_index[id(p.material)]
             if p.area_light is not None and not aggregate_only:
                 if id(p.area_light) not in light_index:

@@ -109,3 +109,20 @@ def test_render_task_range_is_checked(lib):
         with pytest.raises(abi.PbrtError) as e:
             r.render(scene, tasks=(lo, hi))
         assert e.value.status == 1 and b"task range" in lib.pbrtgpu_last_error()
+
+
+def test_host_build_with_disks_and_cylinders_matches_oracle(lib, oracle):
+    """Analytic shapes refine to one primitive each, with the bounds of
+    disk.rs:68-74 / cylinder.rs:96-100, in the reference's BVH."""
+    from pbrt_rust_gb300.scene import Primitive, Shape
+    from pbrt_rust_gb300.transform import Transform
+    prims, _ = G.ray_soup(200, 1, seed=4)
+    for i in range(12):
+        t = Transform.translate((i * 0.3 - 1.5, 0.2 * i, 0.1)) * Transform.rotate(30.0 * i, (1.0, 0.5, 0.0))
+        s = (Shape.disk(t, None, False, 0.1 * i, 0.3, 0.05 * (i % 3), 360.0 - 20.0 * i) if i % 2
+             else Shape.cylinder(t, None, i % 4 == 0, 0.2, -0.3, 0.1 * i, 360.0 - 25.0 * i))
+        prims.append(Primitive.simple(s))
+    g = GpuBVHAccel(prims, 4, "sah")
+    o = oracle.OracleBVH(prims, 4, "sah")
+    assert np.array_equal(g.nodes().view(np.uint8), o.nodes().view(np.uint8))
+    assert np.array_equal(g.primitive_order(), o.primitive_order())

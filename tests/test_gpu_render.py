@@ -10,7 +10,7 @@ import pytest
 
 from pbrt_rust_gb300 import generators as G
 from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
-from pbrt_rust_gb300.scene import (Camera, Film, Filter, SceneDescription, StratifiedSampler,
+from pbrt_rust_gb300.scene import (Camera, Film, Filter, MatteMaterial, SceneDescription, StratifiedSampler,
                                    default_num_tasks)
 
 pytestmark = pytest.mark.gpu
@@ -145,3 +145,18 @@ def test_scene_file_renders_on_the_device(oracle, tmp_path):
                         frame.camera, frame.sampler, frame.num_tasks)
     assert_image_close(gpu, ref)
     assert (tmp_path / "out.png").stat().st_size > 40 * 32 * 3
+
+
+def test_disk_and_cylinder_scene_matches_oracle(oracle):
+    """Shading of disks (the transformed +-z normal, disk.rs:125-129) and
+    cylinders (helpers.rs:17-43) in the plain render scene."""
+    from pbrt_rust_gb300.scene import Primitive, Shape
+    from pbrt_rust_gb300.transform import Transform
+    prims, lights, cam, smp = G.c1_scene(res=64, n_spheres=0)
+    for i in range(6):
+        t = Transform.translate((i - 2.5, 0.6, (i % 3) * 0.8 - 0.8)) * Transform.rotate(-90.0 + 25.0 * i, (1, 0, 0))
+        s = (Shape.disk(t, None, i % 4 == 1, 0.0, 0.45, 0.1, 360.0) if i % 2
+             else Shape.cylinder(t, None, False, 0.3, -0.4, 0.4, 360.0))
+        prims.append(Primitive.geometric(s, MatteMaterial((0.3 + 0.1 * i, 0.5, 0.7 - 0.1 * i))))
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert_image_close(gpu, ref)

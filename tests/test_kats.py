@@ -450,6 +450,82 @@ def test_sphere_dg_kat(oracle):
     assert dpdv[0] == 0.0 and dpdv[1] == 0.0 and abs(dpdv[2] - math.pi / 2) < 1e-6
 
 
+def _quad(oracle, kind, o2w: Transform, a, b, c, pm, rr, mode=0):
+    out = np.zeros(16, np.float32)
+    ta = o2w.to_abi()
+    ok = oracle.load().oracle_quadric_intersect(kind, C.byref(ta), a, b, c, pm, ptr(rr), mode, ptr(out))
+    return out if ok else None
+
+
+def test_disk_intersect_kats(oracle):
+    """src/shape/disk.rs:187-240 (height, radius, inner radius, phi max)."""
+    from pbrt_rust_gb300 import abi
+    D, I = abi.SHAPE_DISK, Transform()
+    down = (0.0, 0.0, -1.0)
+    hit = lambda xf, h, r, ri, pm, o, d=down: _quad(oracle, D, xf, h, r, ri, pm, ray(o, d)) is not None  # noqa
+    assert hit(I, 0.0, 1.0, 0.0, 360.0, (0, 0, 1))
+    assert not hit(I, 0.0, 1.0, 0.0, 360.0, (2, 2, 1))
+    assert not hit(I, 0.0, 1.0, 0.5, 360.0, (0, 0, 1))  # through the hole
+    assert not hit(I, 2.0, 1.0, 0.0, 360.0, (0, 0, 1))  # starting behind it
+    assert hit(I, 0.0, 0.75, 0.25, 180.0, (0, 0.5, 1))  # top half of a half pipe
+    assert not hit(I, 0.0, 0.75, 0.25, 180.0, (0, -0.5, 1))
+    rz = Transform.rotate(180.0, (0.0, 0.0, 1.0))
+    assert not hit(rz, 0.0, 0.75, 0.25, 180.0, (0, 0.5, 1))
+    assert hit(rz, 0.0, 0.75, 0.25, 180.0, (0, -0.5, 1))
+    assert not hit(rz, 0.0, 0.75, 0.25, 180.0, (1.0, 10.5, 140.0), (-1.0, -10.5, -140.0))
+
+
+def test_disk_dg_kats(oracle):
+    """src/shape/disk.rs:242-276."""
+    from pbrt_rust_gb300 import abi
+    o = _quad(oracle, abi.SHAPE_DISK, Transform(), 0.0, 1.0, 0.0, 360.0, ray((0, 0, 1), (0, 0, -1)), mode=1)
+    assert o[0] == 1.0 and o[1] == F(5e-4)
+    assert o[2:5].tolist() == [0.0, 0.0, 0.0] and o[5:8].tolist() == [0.0, 0.0, 1.0]
+    o = _quad(oracle, abi.SHAPE_DISK, Transform(), 0.0, 0.75, 0.25, 180.0, ray((0, 0.5, 1), (0, 0, -1)), mode=1)
+    assert o[0] == 1.0 and o[1] == F(5e-4)
+    assert o[2:5].tolist() == [0.0, 0.5, 0.0] and o[5:8].tolist() == [0.0, 0.0, 1.0]
+    assert o[8] == 0.5 and o[9] == 0.5
+
+
+def test_cylinder_intersect_kats(oracle):
+    """src/shape/cylinder.rs:222-296 (radius, z0, z1, phi max)."""
+    from pbrt_rust_gb300 import abi
+    Y, I = abi.SHAPE_CYLINDER, Transform()
+    hit = lambda xf, r, z0, z1, pm, o, d: _quad(oracle, Y, xf, r, z0, z1, pm, ray(o, d)) is not None  # noqa
+    assert hit(I, 0.5, -1.0, 1.0, 360.0, (1, 1, 1), (-1, -1, -1))
+    assert not hit(I, 0.5, -1.0, 1.0, 360.0, (1, 1, 1), (0, 0, -1))
+    assert not hit(I, 0.5, -1.0, 1.0, 360.0, (1, 1, 2), (-1, -1, 0))
+    assert not hit(I, 0.5, -1.0, 1.0, 360.0, (-1, 1, -2), (1, -1, 0))
+    assert not hit(I, 0.5, -1.0, 1.0, 360.0, (0.1, 0.1, -2), (0, 0, 1))  # down the middle
+    assert hit(I, 0.5, -1.0, 1.0, 360.0, (0.1, 0.1, -2), (-0.4, -0.4, 1.5))  # from the inside
+    xf = Transform.translate((1.0, 2.0, 3.0))
+    assert hit(xf, 1.0, -3.0, 0.0, 90.0, (2, 4, 1.5), (-1, -1, 0))
+    assert not hit(xf, 1.0, -3.0, 0.0, 90.0, (1, 2, 1.5), (-1, -1, 0))
+    assert hit(xf, 1.0, -3.0, 0.0, 90.0, (1, 2, 1.5), (1, 1, 0))
+    assert not hit(xf, 1.0, -3.0, 0.0, 90.0, (2.5, 2.5, 10), (-1, -1, -10))  # barely misses
+    for pm in (360.0, 0.1, 0.0, -1.0):  # no radius, any phi max
+        assert hit(I, 0.0, -1.0, 1.0, pm, (1, 1, -0.5), (-1, -1, 0))
+    assert hit(I, 0.0, 0.0, 0.0, 360.0, (1, 1, 1), (-1, -1, -1))
+    assert not hit(I, 0.0, -1.0, -1.0, 360.0, (1, 1, 1), (-1, -1, -1))
+
+
+def test_cylinder_dg_kat(oracle):
+    """src/shape/cylinder.rs:298-327."""
+    from pbrt_rust_gb300 import abi
+    xf = Transform.rotate(90.0, (0.0, 1.0, 0.0))
+    d = np.array([0.0, -1.0, -1.0], np.float32)
+    d = d * (F(1.0) / np.sqrt(F(d @ d)))
+    o = _quad(oracle, abi.SHAPE_CYLINDER, xf, 1.0, -1.0, 1.0, 180.0, ray((0, 1, 1), tuple(d)), mode=1)
+    t = math.sqrt(2.0) - 1.0
+    assert abs(o[0] - t) < 1e-6 and abs(o[1] - t * 5e-4) < 1e-6
+    s2 = math.sqrt(2.0) * 0.5
+    assert np.sum((o[2:5] - [0.0, s2, s2]) ** 2) < 1e-6
+    assert np.sum((o[5:8] - np.array([0.0, 1.0, 1.0]) / math.sqrt(2.0)) ** 2) < 1e-6
+    assert o[8] == 0.75 and abs(o[9] - 0.5) < 1e-6
+    assert np.sum((o[10:13] - [0.0, -math.pi * s2, math.pi * s2]) ** 2) < 1e-6
+    assert np.sum((o[13:16] - [2.0, 0.0, 0.0]) ** 2) < 1e-6
+
+
 # ------------------------------------------------------------------- BVH ----
 def sphere_at(v):
     """src/primitive/aggregates/mod.rs:76-80"""
