@@ -122,7 +122,15 @@ typedef struct PbrtSceneDesc {
     uint32_t n_lights;
     uint32_t max_prims_in_node;   /* BVHAccelerator::new mp (bvh.rs:335) */
     int32_t split_method;         /* PBRT_SPLIT_* */
+    uint32_t build_flags;         /* PBRT_BUILD_* */
 } PbrtSceneDesc;
+
+/* Build flags.  PBRT_BUILD_ON_DEVICE: the BVH tree (bvh.rs:86-258) is built
+ * by CUDA kernels instead of on the host; same nodes and primitive order
+ * (bit for bit where the host's fmin/fmax order -0 below +0, as on Arm; on
+ * x86 hosts the sign of a zero bound may differ).  The equal-counts split
+ * method stays on the host. */
+enum { PBRT_BUILD_ON_DEVICE = 1 };
 
 /* Perspective camera (src/camera/mod.rs:105-135) with an image film
  * (src/camera/film.rs:77-122) and a box filter (src/filter.rs:45-50). */
@@ -195,6 +203,10 @@ const char* pbrtgpu_last_error(void);
 int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
                        uint32_t max_prims_in_node, const char* split_method,
                        PbrtBVH** out);
+/* pbrtgpu_bvh_create with PBRT_BUILD_* flags (no counterpart in the
+ * reference). */
+int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims,
+                          const char* split_method, uint32_t flags, PbrtBVH** out);
 void pbrtgpu_bvh_destroy(PbrtBVH* bvh);
 
 /* Replaces HasBounds::world_bound for BVHAccelerator (bvh.rs:365-373). */

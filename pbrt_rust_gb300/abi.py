@@ -28,6 +28,7 @@ SHAPE_CYLINDER = 3
 LIGHT_POINT = 0
 LIGHT_DIFFUSE_AREA = 1
 SPLIT_METHODS = {"sah": 0, "middle": 1, "equal": 2}
+BUILD_ON_DEVICE = 1
 
 # 32-byte ray and 16-byte hit records (PbrtRay / PbrtHit).
 RAY_DTYPE = np.dtype([("o", "<f4", 3), ("tmin", "<f4"), ("d", "<f4", 3), ("tmax", "<f4")])
@@ -72,7 +73,7 @@ class PbrtSceneDesc(C.Structure):
         ("shapes", C.POINTER(PbrtShapeDesc)), ("n_shapes", C.c_uint32),
         ("materials", C.POINTER(PbrtMaterialDesc)), ("n_materials", C.c_uint32),
         ("lights", C.POINTER(PbrtLightDesc)), ("n_lights", C.c_uint32),
-        ("max_prims_in_node", C.c_uint32), ("split_method", C.c_int32),
+        ("max_prims_in_node", C.c_uint32), ("split_method", C.c_int32), ("build_flags", C.c_uint32),
     ]
 
 
@@ -155,6 +156,8 @@ SIGNATURES = {
     "pbrtgpu_last_error": (C.c_char_p, []),
     "pbrtgpu_bvh_create": (C.c_int, [C.POINTER(PbrtShapeDesc), C.c_uint32, C.c_uint32, C.c_char_p,
                                      C.POINTER(_P)]),
+    "pbrtgpu_bvh_create_ex": (C.c_int, [C.POINTER(PbrtShapeDesc), C.c_uint32, C.c_uint32, C.c_char_p, C.c_uint32,
+                                        C.POINTER(C.c_void_p)]),
     "pbrtgpu_bvh_destroy": (None, [_P]),
     "pbrtgpu_bvh_world_bound": (C.c_int, [_P, _F3, _F3]),
     "pbrtgpu_bvh_num_primitives": (C.c_int, [_P, _U32P]),

@@ -20,7 +20,8 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libpbrt_gb300.so"
 
 GENCODE = "arch=compute_103a,code=sm_103a"
-CUDA_SOURCES = ["trace.cu", "reorder.cu", "render.cu", "batch.cu", "batch_trace.cu", "capi.cu", "capi_render.cu",
+CUDA_SOURCES = ["trace.cu", "reorder.cu", "render.cu", "batch.cu", "batch_trace.cu", "bvh_build.cu", "capi.cu",
+                "capi_render.cu",
                 "capi_noalloc.cu", "capi_batch.cu", "server.cu"]
 HOST_SOURCES = ["host_scene.cpp", "image_io.cpp"]
 

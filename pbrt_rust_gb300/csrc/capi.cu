@@ -285,11 +285,19 @@ const char* pbrtgpu_last_error(void) { return pbrt::g_last_error.c_str(); }
 
 int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
                        PbrtBVH** out) {
+    return pbrtgpu_bvh_create_ex(shapes, n_shapes, max_prims, split_method, 0, out);
+}
+
+int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims,
+                          const char* split_method, uint32_t flags, PbrtBVH** out) {
     if (!out || (!shapes && n_shapes)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
+    if (flags & ~(uint32_t)PBRT_BUILD_ON_DEVICE) return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown build flags");
+    const bool on_device = (flags & PBRT_BUILD_ON_DEVICE) != 0;
+    if (on_device && !cuda_device_present()) return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device for the build");
     PbrtBVH* b = new PbrtBVH();
     std::string err;
-    int st = build_host_bvh(shapes, n_shapes, max_prims, split_method, &b->host, &err);
+    int st = build_host_bvh(shapes, n_shapes, max_prims, split_method, &b->host, &err, on_device);
     if (st) {
         delete b;
         return set_error(st, err);

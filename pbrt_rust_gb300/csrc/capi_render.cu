@@ -192,7 +192,16 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
     PbrtScene* S = new PbrtScene();
     S->bvh = new PbrtBVH();
     std::string err;
-    int st = build_host_bvh(d->shapes, d->n_shapes, d->max_prims_in_node, sm, &S->bvh->host, &err);
+    if (d->build_flags & ~(uint32_t)PBRT_BUILD_ON_DEVICE) {
+        delete S;
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown build flags");
+    }
+    const bool on_device = (d->build_flags & PBRT_BUILD_ON_DEVICE) != 0;
+    if (on_device && !cuda_device_present()) {
+        delete S;
+        return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device for the build");
+    }
+    int st = build_host_bvh(d->shapes, d->n_shapes, d->max_prims_in_node, sm, &S->bvh->host, &err, on_device);
     if (st) {
         delete S;
         return set_error(st, err);

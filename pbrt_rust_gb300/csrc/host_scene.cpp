@@ -235,13 +235,13 @@ struct Task {
 
 }  // namespace
 
-static int build_tree(HostBVH& H, uint32_t mp, int split, std::string* err) {
+void prim_bounds(const HostBVH& H, std::vector<Box>* bounds, std::vector<float>* cx, std::vector<float>* cy,
+                 std::vector<float>* cz) {
     const size_t n = H.prims.size();
-    H.nodes.clear();
-    H.ordered.resize(n);
-    if (n == 0) return PBRT_OK;
-    std::vector<Box> bounds(n);
-    std::vector<float> cx(n), cy(n), cz(n);
+    bounds->resize(n);
+    cx->resize(n);
+    cy->resize(n);
+    cz->resize(n);
     for (size_t i = 0; i < n; ++i) {
         const HostPrim& p = H.prims[i];
         Box b;
@@ -253,13 +253,23 @@ static int build_tree(HostBVH& H, uint32_t mp, int split, std::string* err) {
             std::memcpy(o2w.m, s.o2w, sizeof(o2w.m));
             b = xf_box(o2w, Box{v3(-s.radius, -s.radius, s.z_min), v3(s.radius, s.radius, s.z_max)});
         }
-        bounds[i] = b;
+        (*bounds)[i] = b;
         V3 c = (b.lo + b.hi) * 0.5f;  // bvh.rs:77
-        cx[i] = c.x;
-        cy[i] = c.y;
-        cz[i] = c.z;
-        H.ordered[i] = (uint32_t)i;
+        (*cx)[i] = c.x;
+        (*cy)[i] = c.y;
+        (*cz)[i] = c.z;
     }
+}
+
+static int build_tree(HostBVH& H, uint32_t mp, int split, std::string* err) {
+    const size_t n = H.prims.size();
+    H.nodes.clear();
+    H.ordered.resize(n);
+    if (n == 0) return PBRT_OK;
+    std::vector<Box> bounds;
+    std::vector<float> cx, cy, cz;
+    prim_bounds(H, &bounds, &cx, &cy, &cz);
+    for (size_t i = 0; i < n; ++i) H.ordered[i] = (uint32_t)i;
     const float* cent[3] = {cx.data(), cy.data(), cz.data()};
     uint32_t* idx = H.ordered.data();
     H.nodes.reserve(2 * n);
@@ -521,7 +531,7 @@ static void fill_node4_layout(HostBVH& H) {
 }
 
 int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
-                   HostBVH* out, std::string* err) {
+                   HostBVH* out, std::string* err, bool on_device) {
     HostBVH& H = *out;
     H = HostBVH();
     // Full refinement: primitive/mod.rs:47-63, mesh.rs:298-338.
@@ -622,7 +632,11 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
             return PBRT_ERR_INVALID_ARGUMENT;
         }
     }
-    int st = build_tree(H, max_prims, parse_split_method(split_method), err);
+    const int split = parse_split_method(split_method);
+    // equal-counts splits of large ranges use the sequential partition_by
+    // (utils/mod.rs:112-169), which stays on the host
+    int st = (on_device && split != PBRT_SPLIT_EQUAL) ? device_build_tree(H, max_prims, split, err)
+                                                      : build_tree(H, max_prims, split, err);
     if (st) return st;
     fill_device_layout(H);
     fill_node4_layout(H);

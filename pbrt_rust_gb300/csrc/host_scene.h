@@ -98,7 +98,16 @@ struct HostBVH {
 // Fully refine shapes, build and flatten the BVH, and fill the device
 // layout.  Returns a PbrtStatus; *err gets a message on failure.
 int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
-                   HostBVH* out, std::string* err);
+                   HostBVH* out, std::string* err, bool on_device = false);
+
+// Bounds (mesh.rs:196-205, sphere.rs:111-126) and centroids (bvh.rs:77) of
+// the refined primitives.
+void prim_bounds(const HostBVH& H, std::vector<Box>* bounds, std::vector<float>* cx, std::vector<float>* cy,
+                 std::vector<float>* cz);
+
+// The tree of build_tree (H.nodes, H.ordered, H.depth) built on the current
+// CUDA device (bvh_build.cu): identical nodes and primitive order.
+int device_build_tree(HostBVH& H, uint32_t max_prims, int split, std::string* err);
 
 int parse_split_method(const char* s);
 

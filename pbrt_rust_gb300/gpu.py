@@ -65,7 +65,10 @@ class GpuBVHAccel:
     Shape); every mesh refines to its triangles in index order, and hit
     indices refer to that refined list."""
 
-    def __init__(self, prims, max_prims: int = 4, split_method: str = "sah", _handle=None, _owner=None):
+    def __init__(self, prims, max_prims: int = 4, split_method: str = "sah", _handle=None, _owner=None,
+                 build_on_device: bool = False):
+        """``build_on_device`` builds the tree with CUDA kernels (same
+        result as the host build)."""
         self._lib = abi.load()
         self._owner = _owner
         if _handle is not None:
@@ -76,8 +79,10 @@ class GpuBVHAccel:
         prims = [p if isinstance(p, Primitive) else Primitive.simple(p) for p in prims]
         self.desc = SceneDescription(prims, [], max_prims, split_method, aggregate_only=True)
         h = C.c_void_p()
-        abi.check(self._lib.pbrtgpu_bvh_create(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
-                                               split_method.encode(), C.byref(h)), self._lib)
+        abi.check(self._lib.pbrtgpu_bvh_create_ex(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
+                                                  split_method.encode(),
+                                                  abi.BUILD_ON_DEVICE if build_on_device else 0, C.byref(h)),
+                  self._lib)
         self._h = h
         self._own = True
 
@@ -165,9 +170,11 @@ class GpuScene:
     """Scene::new_with (src/scene.rs:31-39) on the device: the aggregate
     plus materials and lights."""
 
-    def __init__(self, prims: list[Primitive], lights: list = (), max_prims: int = 4, split_method: str = "sah"):
+    def __init__(self, prims: list[Primitive], lights: list = (), max_prims: int = 4, split_method: str = "sah",
+                 build_on_device: bool = False):
         self._lib = abi.load()
         self.desc = SceneDescription(prims, lights, max_prims, split_method)
+        self.desc.desc.build_flags = abi.BUILD_ON_DEVICE if build_on_device else 0
         h = C.c_void_p()
         abi.check(self._lib.pbrtgpu_scene_create(C.byref(self.desc.desc), C.byref(h)), self._lib)
         self._h = h
