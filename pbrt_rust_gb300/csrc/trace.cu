@@ -181,7 +181,111 @@ __global__ void __launch_bounds__(128, MINB)
     if (overflow) atomicMax(status, 6);
 }
 
-enum { kVariantPairPlain = 0, kVariantPairPersistent = 1, kVariantWidePlain = 2, kVariantWidePersistent = 3 };
+// 4-wide persistent traversal with postponed leaves.  A lane that reaches a
+// leaf keeps it aside and carries on down its stack; the warp tests the kept
+// leaves together once enough lanes are stuck behind a second leaf (or have
+// nothing else left), so the leaf code runs with many lanes instead of one
+// or two.  A kept leaf is always tested before the lane's next leaf, so
+// primitives are still tested in the reference's depth-first order; the
+// nodes a lane visits while a leaf is kept are tested against a maxt that
+// the kept leaf may still shrink, so some nodes the reference culls are
+// visited too - their primitives are all farther than the closest hit - and
+// the result, ties included, is the reference's.  Work comes from the
+// shared counter (chunks of per_warp rays) or from fixed per-warp ranges.
+template <int SMAX, int OVF, bool ANY>
+__global__ void __launch_bounds__(128)
+    k_trace4_spec(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ order,
+                  float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status, uint32_t per_warp,
+                  uint32_t refill, uint32_t* __restrict__ work) {
+    extern __shared__ uint2 smem_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t next = work ? 0 : warp * per_warp;
+    uint64_t end = work ? 0 : ((next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n);
+    bool more = work != nullptr;
+    const uint32_t kNone = 0xffffffffu;
+    uint32_t ray = kNone;
+    uint32_t kept = kNone;  // postponed leaf
+    bool live = false;      // `T.cur` holds the next node or leaf
+    bool overflow = false;
+    DRay r;
+    Traversal4<SMAX, OVF> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    auto finish = [&]() {
+        overflow |= T.overflow;
+        if (ANY)
+            occ[ray] = T.found ? 1 : 0;
+        else
+            hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        ray = kNone;
+        kept = kNone;
+        live = false;
+    };
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
+        const unsigned nidle = __popc(idle);
+        if (more && next >= end && nidle >= refill) {  // warp-uniform
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, per_warp);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base < n) {
+                next = base;
+                end = (uint64_t)base + per_warp < (uint64_t)n ? (uint64_t)base + per_warp : (uint64_t)n;
+            } else {
+                more = false;
+            }
+        }
+        const bool tail = !more && next + nidle >= end;
+        if (next < end && nidle >= (tail ? 1u : refill)) {
+            if (ray == kNone) {
+                const uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
+                if (my < end) {
+                    ray = order ? __ldg(order + my) : (uint32_t)my;
+                    r = make_dray(__ldg(rays + 2 * (size_t)ray), __ldg(rays + 2 * (size_t)ray + 1));
+                    live = T.start(bvh, r);
+                    if (!live) finish();
+                }
+            }
+            next += nidle;
+        }
+        const bool busy = ray != kNone;
+        if (!__any_sync(0xffffffffu, busy)) {
+            if (next >= end && !more) break;
+            continue;
+        }
+        const bool at_leaf = busy && live && (T.cur & kNode4Leaf);
+        const bool blocked = busy && kept != kNone && (at_leaf || !live);
+        const unsigned nbusy = __popc(__ballot_sync(0xffffffffu, busy));
+        const unsigned nblocked = __popc(__ballot_sync(0xffffffffu, blocked));
+        const unsigned nkept = __popc(__ballot_sync(0xffffffffu, busy && kept != kNone));
+        if (nblocked && (4 * nblocked >= nbusy || nkept == nbusy)) {
+            // leaf round: every kept leaf is tested now
+            if (busy && kept != kNone) {
+                const bool stop = T.template leaf<ANY>(bvh, r, kept);
+                kept = kNone;
+                if (stop || T.overflow) finish();
+            }
+        } else if (busy && live && !blocked) {  // a blocked lane waits for the leaf round
+            if (at_leaf) {  // keep it, go on with the next stack entry
+                kept = T.cur;
+                live = T.pop();
+            } else {
+                live = T.node(bvh, r);
+                if (T.overflow) finish();
+            }
+        }
+        if (ray != kNone && !live && kept == kNone) finish();
+    }
+    if (overflow) atomicMax(status, 6);
+}
+
+enum {
+    kVariantPairPlain = 0,
+    kVariantPairPersistent = 1,
+    kVariantWidePlain = 2,
+    kVariantWidePersistent = 3,
+    kVariantWideSpeculative = 4
+};
 static int g_kernel_variant = -1;
 static unsigned g_refill = 4;
 static unsigned g_min_blocks = 0;
@@ -194,6 +298,7 @@ static int variant_from_name(const char* v, int dflt) {
     if (!strcmp(v, "pt")) return kVariantPairPersistent;
     if (!strcmp(v, "w4")) return kVariantWidePlain;
     if (!strcmp(v, "w4pt")) return kVariantWidePersistent;
+    if (!strcmp(v, "w4spec")) return kVariantWideSpeculative;
     return dflt;
 }
 
@@ -257,6 +362,37 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
 }
 
 template <int SMAX, int OVF, bool ANY>
+static cudaError_t launch_wide_spec(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
+                                    float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream, uint32_t* work) {
+    const int block = 128;
+    const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
+    static int bps = 0, sms = 0;
+    if (bps == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_spec<SMAX, OVF, ANY>, block, smem);
+        if (bps < 1) bps = 1;
+    }
+    const uint64_t warps = (uint64_t)sms * bps * (block / 32);
+    if (work && g_chunk && n <= 0xF0000000u) {
+        const uint64_t chunks = (n + g_chunk - 1) / g_chunk;
+        const uint64_t w = chunks < warps ? chunks : warps;
+        const unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
+        k_trace4_spec<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status, g_chunk,
+                                                                   g_refill, work);
+        return cudaGetLastError();
+    }
+    uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
+    if (per_warp < 32) per_warp = 32;
+    const uint64_t need_warps = (n + per_warp - 1) / per_warp;
+    const unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
+    k_trace4_spec<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status, per_warp,
+                                                               g_refill, nullptr);
+    return cudaGetLastError();
+}
+
+template <int SMAX, int OVF, bool ANY>
 static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order, float4* h4,
                                uint8_t* occ, int* d_status, cudaStream_t stream, bool persistent, uint32_t* work) {
     const int block = 128;
@@ -274,7 +410,7 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
 }
 
 int set_trace_config(const PbrtTraceConfig& c) {
-    if (c.kernel < kVariantPairPlain || c.kernel > kVariantWidePersistent || c.refill < 1 || c.refill > 32) return 1;
+    if (c.kernel < kVariantPairPlain || c.kernel > kVariantWideSpeculative || c.refill < 1 || c.refill > 32) return 1;
     if (!(c.min_blocks == 0 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
     if (c.render_kernel != kVariantPairPlain && c.render_kernel != kVariantWidePlain) return 1;
     if (c.reorder > 1) return 1;
@@ -352,6 +488,18 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     if (n == 0) return cudaSuccess;
     read_variant();
     const int variant = kernel >= 0 ? kernel : g_kernel_variant;
+    if (wide && variant == kVariantWideSpeculative) {
+        const float4* r4 = reinterpret_cast<const float4*>(rays);
+        float4* h4 = reinterpret_cast<float4*>(hits);
+        const bool any = occluded != nullptr;
+        const int v = wide_stack_variant(wide_bound);
+        if (v == 64)
+            return any ? launch_wide_spec<16, 48, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, work)
+                       : launch_wide_spec<16, 48, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, work);
+        if (v == 256)
+            return any ? launch_wide_spec<16, 240, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, work)
+                       : launch_wide_spec<16, 240, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, work);
+    }
     if (wide && (variant == kVariantWidePlain || variant == kVariantWidePersistent)) {
         const float4* r4 = reinterpret_cast<const float4*>(rays);
         float4* h4 = reinterpret_cast<float4*>(hits);

@@ -123,36 +123,50 @@ struct Traversal4 {
         return false;
     }
 
+    // Tests the primitives of leaf `ref` (a kNode4Leaf child word) in
+    // order; true if ANY and one was hit.
+    template <bool ANY>
+    __device__ __forceinline__ bool leaf(const DevBVH4& bvh, const DRay& r, uint32_t ref) {
+        uint32_t off = ref & ~kNode4Leaf;
+        for (;;) {
+            const PrimRec* pr = bvh.prims + off;
+            float4 r0 = ldg4(pr->r0);
+            float4 r1 = ldg4(pr->r1);
+            float4 r2 = ldg4(pr->r2);
+            uint32_t id = __float_as_uint(r0.w);
+            float t, b1 = 0.0f, b2 = 0.0f;
+            bool hit;
+            if (id & kSphereBit)
+                hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
+            else
+                hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
+            if (hit) {
+                maxt = t;
+                found = true;
+                res.prim = (int32_t)(id & ~kSphereBit);
+                res.t = t;
+                res.b1 = b1;
+                res.b2 = b2;
+                if (ANY) return true;
+            }
+            if (__float_as_uint(r2.w) & kPrimLastBit) return false;
+            ++off;
+        }
+    }
+
     template <bool ANY>
     __device__ __forceinline__ bool step(const DevBVH4& bvh, const DRay& r) {
         if (cur & kNode4Leaf) {
-            uint32_t off = cur & ~kNode4Leaf;
-            for (;;) {
-                const PrimRec* pr = bvh.prims + off;
-                float4 r0 = ldg4(pr->r0);
-                float4 r1 = ldg4(pr->r1);
-                float4 r2 = ldg4(pr->r2);
-                uint32_t id = __float_as_uint(r0.w);
-                float t, b1 = 0.0f, b2 = 0.0f;
-                bool hit;
-                if (id & kSphereBit)
-                    hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
-                else
-                    hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
-                if (hit) {
-                    maxt = t;
-                    found = true;
-                    res.prim = (int32_t)(id & ~kSphereBit);
-                    res.t = t;
-                    res.b1 = b1;
-                    res.b2 = b2;
-                    if (ANY) return false;
-                }
-                if (__float_as_uint(r2.w) & kPrimLastBit) break;
-                ++off;
-            }
+            if (leaf<ANY>(bvh, r, cur)) return false;
             return pop();
         }
+        return node(bvh, r);
+    }
+
+    // Visits inner node `cur`: tests its children and moves `cur` to the
+    // next node or leaf in the reference's order; false once nothing is
+    // left.
+    __device__ __forceinline__ bool node(const DevBVH4& bvh, const DRay& r) {
         const Node4* nd = bvh.nodes + cur;
         ChildV c0 = ld_child(&nd->c[0]), c1 = ld_child(&nd->c[1]);
         ChildV c2 = ld_child(&nd->c[2]), c3 = ld_child(&nd->c[3]);

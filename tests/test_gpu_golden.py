@@ -25,7 +25,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-@pytest.fixture(params=["plain", "pt", "w4", "w4pt"])
+@pytest.fixture(params=["plain", "pt", "w4", "w4pt", "w4spec"])
 def kernel(request):
     before = abi.get_trace_config()
     abi.set_trace_config(kernel=request.param)

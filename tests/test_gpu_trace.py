@@ -79,7 +79,7 @@ def assert_hits_match(oracle_bvh, got, want, rays, check_f64=True):
             assert abs(got["t"][i] - t64) <= 1e-5 * abs(t64), (i, got["t"][i], t64)
 
 
-KERNELS = ["plain", "pt", "w4", "w4pt"]
+KERNELS = ["plain", "pt", "w4", "w4pt", "w4spec"]
 
 
 @pytest.fixture(params=KERNELS)
