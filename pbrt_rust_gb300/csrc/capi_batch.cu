@@ -30,7 +30,7 @@ size_t up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
 // Byte layout of the device arena and of the upload block inside it.
 struct Layout {
-    size_t rays, hits, img, le, L;                  // per sample
+    size_t rays, hits, img, pixbox, le, L;          // per sample (pixbox: per pixel, pixels <= samples)
     size_t lsamp, contrib, occ, qrays, qslot, qjob;  // per light sample
     size_t counters;
     size_t upload, o_pix, o_ray, o_smp, o_film, o_jobs, o_tables, o_tasks, upload_bytes;
@@ -49,6 +49,7 @@ struct Layout {
         rays = take(S * sizeof(PbrtRay));
         hits = take(S * 16);
         img = take(S * 8);
+        pixbox = take(S * 16);
         le = take(S * 16);
         L = take(S * 16);
         lsamp = take(SL * 12);
@@ -387,6 +388,7 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
     P.rays = b->dev<PbrtRay>(Y.rays) + b->n_smp;
     P.hits = b->dev<float4>(Y.hits) + b->n_smp;
     P.img = b->dev<float2>(Y.img) + b->n_smp;
+    P.pixbox = b->dev<float4>(Y.pixbox) + b->n_pix;
     P.le = b->dev<float4>(Y.le) + b->n_smp;
     P.L = b->dev<float4>(Y.L) + b->n_smp;
     P.lsamp = b->dev<float>(Y.lsamp) + 3 * b->n_lsmp;

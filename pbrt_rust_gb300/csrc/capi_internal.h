@@ -73,12 +73,12 @@ struct PbrtScene {
     float* d_area_cdf = nullptr;
     std::atomic<bool> uploaded{false};
     std::mutex mu;  // serialises renders: they share the scratch buffers below
-    pbrt::DeviceBuf rays, hits, img, lsamp, contrib, le, L, srays, sslot, occ, counters, tasks, table, rgb;
+    pbrt::DeviceBuf rays, hits, img, pixbox, lsamp, contrib, le, L, srays, sslot, occ, counters, tasks, table, rgb;
     ~PbrtScene() {
         if (bvh) delete bvh;
         for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lights, (void*)d_area_tris, (void*)d_area_cdf})
             if (p) cudaFree(p);
-        for (pbrt::DeviceBuf* b : {&rays, &hits, &img, &lsamp, &contrib, &le, &L, &srays, &sslot, &occ, &counters,
+        for (pbrt::DeviceBuf* b : {&rays, &hits, &img, &pixbox, &lsamp, &contrib, &le, &L, &srays, &sslot, &occ, &counters,
                                    &tasks, &table, &rgb})
             b->release();
     }

@@ -158,12 +158,13 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     const uint64_t S_ = P.n_samples, SL = P.n_samples * (uint64_t)nl;
     const uint64_t npx = (uint64_t)(P.fx1 - P.fx0) * (uint64_t)(P.fy1 - P.fy0);
     const bool dev_out = is_device_pointer(rgb_out);
-    void *p_rays, *p_hits, *p_img, *p_lsamp, *p_contrib, *p_le, *p_L, *p_srays, *p_sslot, *p_occ, *p_cnt, *p_tasks,
+    void *p_rays, *p_hits, *p_img, *p_pixbox, *p_lsamp, *p_contrib, *p_le, *p_L, *p_srays, *p_sslot, *p_occ, *p_cnt, *p_tasks,
         *p_table, *p_rgb = nullptr;
     auto layout = [&](Carve& c) {
         p_rays = c.take(S_ * sizeof(PbrtRay));
         p_hits = c.take(S_ * 16);
         p_img = c.take(S_ * 8);
+        p_pixbox = c.take((uint64_t)P.n_pixels * 16);
         p_lsamp = c.take(S_ * 3 * nl * 4 + 4);
         p_contrib = c.take(SL * 16 + 16);
         p_le = c.take(S_ * 16);
@@ -211,6 +212,7 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     P.rays = (PbrtRay*)p_rays;
     P.hits = (float4*)p_hits;
     P.img = (float2*)p_img;
+    P.pixbox = (float4*)p_pixbox;
     P.lsamp = (float*)p_lsamp;
     P.contrib = (float4*)p_contrib;
     P.le = (float4*)p_le;

@@ -461,7 +461,8 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
     const uint64_t S_ = P.n_samples, SL = P.n_samples * (uint64_t)nl;
     const uint64_t npx = (uint64_t)(P.fx1 - P.fx0) * (uint64_t)(P.fy1 - P.fy0);
     if ((st = S->rays.reserve(S_ * sizeof(PbrtRay))) || (st = S->hits.reserve(S_ * 16)) ||
-        (st = S->img.reserve(S_ * 8)) || (st = S->lsamp.reserve(S_ * 3 * nl * 4 + 4)) ||
+        (st = S->img.reserve(S_ * 8)) || (st = S->pixbox.reserve((uint64_t)P.n_pixels * 16)) ||
+        (st = S->lsamp.reserve(S_ * 3 * nl * 4 + 4)) ||
         (st = S->contrib.reserve(SL * 16 + 16)) || (st = S->le.reserve(S_ * 16)) || (st = S->L.reserve(S_ * 16)) ||
         (st = S->srays.reserve(SL * sizeof(PbrtRay) + 32)) || (st = S->sslot.reserve(SL * 4 + 4)) ||
         (st = S->occ.reserve(SL + 1)) || (st = S->counters.reserve(64)) ||
@@ -481,6 +482,7 @@ int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const P
     P.rays = (PbrtRay*)S->rays.p;
     P.hits = (float4*)S->hits.p;
     P.img = (float2*)S->img.p;
+    P.pixbox = (float4*)S->pixbox.p;
     P.lsamp = (float*)S->lsamp.p;
     P.contrib = (float4*)S->contrib.p;
     P.le = (float4*)S->le.p;

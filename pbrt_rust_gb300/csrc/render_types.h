@@ -84,6 +84,7 @@ struct RenderParams {
     PbrtRay* rays;
     float4* hits;
     float2* img;
+    float4* pixbox;     // per sampler pixel: (min x, min y, max x, max y) of its sample positions
     float* lsamp;       // 3 * n_lights floats per sample: components then positions
     float4* contrib;    // per (sample, light): rgb, w = 1 if a shadow ray decides it
     float4* le;         // per sample emitted radiance

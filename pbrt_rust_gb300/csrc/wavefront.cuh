@@ -117,12 +117,13 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
     }
     const uint32_t spp = P.spp, nl = P.n_lights;
     const uint64_t s0 = (uint64_t)pix * spp;
-    if (t == P.n_tasks) {  // not covered by any task (cannot happen for a tiling)
+    if (t == P.n_tasks) {  // not covered by any task (another shard's task, or no tiling)
         for (uint32_t i = 0; i < spp; ++i) {
             P.img[s0 + i] = make_float2(-1.0e30f, -1.0e30f);
             PbrtRay r = {0, 0, 0, 1.0f, 0, 0, 1.0f, 0.0f};
             P.rays[s0 + i] = r;
         }
+        P.pixbox[pix] = make_float4(-1.0e30f, -1.0e30f, -1.0e30f, -1.0e30f);
         return;
     }
     const TaskRec& T = P.tasks[t];
@@ -146,6 +147,7 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
             c2w[k] = P.c2w[k];
         }
         const float dx = 1.0f / (float)P.xs, dy = 1.0f / (float)P.ys;
+        float4 bb = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
         for (uint32_t yy = 0; yy < P.ys; ++yy)
             for (uint32_t xx = 0; xx < P.xs; ++xx) {
                 const float jx = jit ? rng.random_float() : 0.5f;
@@ -154,10 +156,12 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
                 const float iy = (((float)yy + jy) * dy) + (float)y;
                 const uint64_t s = s0 + yy * P.xs + xx;
                 P.img[s] = make_float2(ix, iy);
+                bb = make_float4(fminf(bb.x, ix), fminf(bb.y, iy), fmaxf(bb.z, ix), fmaxf(bb.w, iy));
                 PbrtRay r;
                 camera_ray(P, r2c, c2w, ix, iy, 0.0f, 0.0f, &r);
                 P.rays[s] = r;
             }
+        P.pixbox[pix] = bb;
         // lens (2 spp) and time (spp) strata when jittered, then one u64 per
         // element of each shuffle (2 x 2 spp words)
         rng.skip((jit ? 3u * spp : 0u) + 4u * spp);
@@ -181,10 +185,14 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
     stratified_2d(image, P.xs, P.ys, rng, jit);
     stratified_2d(lens, P.xs, P.ys, rng, jit);
     stratified_1d(time, spp, rng, jit);
+    float4 bb = make_float4(FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX);
     for (uint32_t i = 0; i < spp; ++i) {
         image[2 * i] += (float)x;
         image[2 * i + 1] += (float)y;
+        bb = make_float4(fminf(bb.x, image[2 * i]), fminf(bb.y, image[2 * i + 1]), fmaxf(bb.z, image[2 * i]),
+                         fmaxf(bb.w, image[2 * i + 1]));
     }
+    P.pixbox[pix] = bb;
     shuffle(lens, spp, 2, rng);
     shuffle(time, spp, 1, rng);
     for (uint32_t i = 0; i < spp; ++i) {
@@ -487,7 +495,17 @@ __device__ __forceinline__ void film_pixel(const RenderParams& P, uint32_t idx) 
         const int32_t sw = P.sx1 - P.sx0;
         for (int32_t sy = ylo; sy <= yhi; ++sy)
             for (int32_t sx = xlo; sx <= xhi; ++sx) {
-                const uint64_t base = ((uint64_t)(sy - P.sy0) * (uint64_t)sw + (uint64_t)(sx - P.sx0)) * P.spp;
+                const uint64_t sp = (uint64_t)(sy - P.sy0) * (uint64_t)sw + (uint64_t)(sx - P.sx0);
+                // The landing bounds below are non-decreasing in the sample
+                // position, so if the source pixel's extreme samples cannot
+                // land on (px, py), none of its samples can.
+                const float4 bb = P.pixbox[sp];
+                if (dev_f2i32(floorf((bb.z - 0.5f) + P.filter_xw)) < px ||
+                    dev_f2i32(ceilf((bb.x - 0.5f) - P.filter_xw)) > px ||
+                    dev_f2i32(floorf((bb.w - 0.5f) + P.filter_yw)) < py ||
+                    dev_f2i32(ceilf((bb.y - 0.5f) - P.filter_yw)) > py)
+                    continue;
+                const uint64_t base = sp * P.spp;
                 for (uint32_t i = 0; i < P.spp; ++i) {
                     const float2 im = P.img[base + i];
                     // film.rs:198-210 against the task film's extent
