@@ -6,7 +6,7 @@
 // recursion becomes two phases over one array of primitive indices, every
 // node owning a contiguous range of it:
 //
-//   A. ranges above kSmall primitives, one tree level per round: every range
+//   A. ranges above kSmall (32) primitives, one tree level per round: every range
 //      of the level is cut into chunks; chunk kernels reduce its bounds and
 //      centroid bounds, fill the twelve SAH buckets (or test the middle
 //      split) and count the left side, one thread per range picks the split,
@@ -37,7 +37,12 @@ namespace pbrt {
 
 namespace {
 
-constexpr uint32_t kSmall = 256;  // ranges of at most this many primitives go to phase B
+#ifndef PBRT_BUILD_SMALL
+#define PBRT_BUILD_SMALL 32
+#endif
+// ranges of at most this many primitives go to phase B (one thread each:
+// small ranges keep that serial work short and the thread count high)
+constexpr uint32_t kSmall = PBRT_BUILD_SMALL;
 constexpr uint32_t kChunk = 2048; // phase A chunk
 constexpr int kNB = 12;           // SAH buckets (bvh.rs:188)
 
