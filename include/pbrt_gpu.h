@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define PBRT_GPU_ABI_VERSION 1
+#define PBRT_GPU_ABI_VERSION 2
 
 /* Status codes.  The reference signals failures with panic!/assert!
  * (e.g. src/primitive/aggregates/bvh.rs:237-238); here they come back as
@@ -52,7 +52,11 @@ typedef struct PbrtRay {
  * refined input list (every mesh expands to its triangles in index order,
  * src/shape/mesh.rs:325-335 + src/primitive/mod.rs:47-63), -1 on a miss.
  * For triangles b1/b2 are the barycentrics of src/shape/mesh.rs:41-72;
- * for spheres both are 0. */
+ * for spheres both are 0.  With instances (PBRT_SHAPE_INSTANCE) each
+ * instance takes as many indices as its definition has refined
+ * primitives, so prim = the instance's first index + the hit primitive's
+ * refined index inside the definition: the indices the same scene would
+ * give with every instance copied out. */
 typedef struct PbrtHit {
     int32_t prim;
     float t;
@@ -67,7 +71,13 @@ typedef struct PbrtTransform {
     float m_inv[16];
 } PbrtTransform;
 
-enum { PBRT_SHAPE_TRIANGLE_MESH = 0, PBRT_SHAPE_SPHERE = 1, PBRT_SHAPE_DISK = 2, PBRT_SHAPE_CYLINDER = 3 };
+enum {
+    PBRT_SHAPE_TRIANGLE_MESH = 0,
+    PBRT_SHAPE_SPHERE = 1,
+    PBRT_SHAPE_DISK = 2,
+    PBRT_SHAPE_CYLINDER = 3,
+    PBRT_SHAPE_INSTANCE = 4 /* TransformedPrimitive (src/primitive/transformed.rs:14-59) */
+};
 enum { PBRT_SPLIT_SAH = 0, PBRT_SPLIT_MIDDLE = 1, PBRT_SPLIT_EQUAL = 2 };
 
 /* One input primitive.  Mirrors Shape::triangle_mesh and Shape::sphere
@@ -90,6 +100,10 @@ typedef struct PbrtShapeDesc {
      * phi_max_deg */
     float radius, z0, z1, phi_max_deg;
     float height, inner_radius;
+    /* instance: index into PbrtSceneDesc.instances; object_to_world places
+     * the definition in the world (its inverse is the world-to-primitive
+     * transform of TransformedPrimitive) */
+    int32_t instance;
     /* render-only */
     int32_t material;             /* index into PbrtSceneDesc.materials */
     int32_t area_light;           /* index into PbrtSceneDesc.lights or -1 */
@@ -113,6 +127,16 @@ typedef struct PbrtLightDesc {
     int32_t shape;                /* area: index of the emitting mesh shape */
 } PbrtLightDesc;
 
+/* One object definition (ObjectBegin ... ObjectEnd): its shapes in
+ * instance space, materials indexing the scene's table.  Definitions hold
+ * no instances and no area lights.  Every PBRT_SHAPE_INSTANCE shape of the
+ * scene is one primitive of the scene's BVH whose own BVH over the
+ * definition is shared by all its instances. */
+typedef struct PbrtInstanceDesc {
+    const PbrtShapeDesc* shapes;
+    uint32_t n_shapes;
+} PbrtInstanceDesc;
+
 typedef struct PbrtSceneDesc {
     const PbrtShapeDesc* shapes;
     uint32_t n_shapes;
@@ -123,6 +147,8 @@ typedef struct PbrtSceneDesc {
     uint32_t max_prims_in_node;   /* BVHAccelerator::new mp (bvh.rs:335) */
     int32_t split_method;         /* PBRT_SPLIT_* */
     uint32_t build_flags;         /* PBRT_BUILD_* */
+    const PbrtInstanceDesc* instances;
+    uint32_t n_instances;
 } PbrtSceneDesc;
 
 /* Build flags.  PBRT_BUILD_ON_DEVICE: the BVH tree (bvh.rs:86-258) is built
@@ -207,6 +233,12 @@ int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
  * reference). */
 int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims,
                           const char* split_method, uint32_t flags, PbrtBVH** out);
+/* The aggregate of a scene description's shapes, instances included
+ * (BVHAccelerator::new over primitives some of which are
+ * TransformedPrimitive, src/primitive/transformed.rs:14-73); uses
+ * max_prims_in_node, split_method, build_flags and the instance
+ * definitions, ignores materials and lights. */
+int pbrtgpu_bvh_create_desc(const PbrtSceneDesc* desc, PbrtBVH** out);
 void pbrtgpu_bvh_destroy(PbrtBVH* bvh);
 
 /* Replaces HasBounds::world_bound for BVHAccelerator (bvh.rs:365-373). */

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -837,7 +838,7 @@ void sphere_dg(const Sphere& s, const Ray& obj_ray, float t_hit, float phi, V3* 
 }
 
 // ----------------------------------------------------------- primitives ---
-enum { KIND_TRI = 0, KIND_SPHERE = 1 };
+enum { KIND_TRI = 0, KIND_SPHERE = 1, KIND_INST = 2 };
 struct Prim {
     int kind;
     int shape;
@@ -847,9 +848,20 @@ struct Prim {
     int sphere;  // index into spheres
 };
 
+// TransformedPrimitive (transformed.rs:14-33) with a static transform:
+// w2p = the instance's world-to-primitive matrix, i2w its inverse as given
+// (Transform::invert swaps the pair, transform.rs:31-33).
+struct Inst {
+    M4 i2w, w2i;
+    int def;  // index into Refined::defs
+};
+
 struct Refined {
     std::vector<Prim> prims;
     std::vector<Sphere> spheres;
+    std::vector<Inst> insts;
+    std::vector<std::shared_ptr<OracleBVH>> defs;  // instance definitions' aggregates
+    std::vector<uint32_t> first_id;  // with instances: the hit id of each refined primitive
     std::string err;
 };
 
@@ -903,6 +915,20 @@ bool refine_shapes(const PbrtShapeDesc* shapes, uint32_t n, Refined* out) {
             p.sphere = (int)out->spheres.size();
             out->spheres.push_back(s);
             out->prims.push_back(p);
+        } else if (d.kind == PBRT_SHAPE_INSTANCE) {
+            if (d.instance < 0 || (size_t)d.instance >= out->defs.size()) {
+                out->err = "instance: definition index out of range";
+                return false;
+            }
+            Prim p;
+            p.kind = KIND_INST;
+            p.shape = (int)si;
+            p.material = -1;
+            p.area_light = -1;
+            p.tri = Tri{};
+            p.sphere = (int)out->insts.size();
+            out->insts.push_back(Inst{o2w.m, o2w.mi, d.instance});
+            out->prims.push_back(p);
         } else {
             out->err = "unknown shape kind";
             return false;
@@ -911,8 +937,17 @@ bool refine_shapes(const PbrtShapeDesc* shapes, uint32_t n, Refined* out) {
     return true;
 }
 
+BBox def_bound(const OracleBVH* o);
+size_t def_size(const OracleBVH* o);
+
 BBox prim_bound(const Refined& R, const Prim& p) {
     if (p.kind == KIND_TRI) return tri_bound(p.tri);
+    if (p.kind == KIND_INST) {
+        // transformed.rs:62-65 + animated.rs:226-233: the definition's
+        // bound through start_transform.inverse() = primitive-to-world
+        const Inst& I = R.insts[p.sphere];
+        return xf_bbox(I.i2w, def_bound(R.defs[I.def].get()));
+    }
     return sphere_bound(R.spheres[p.sphere]);
 }
 
@@ -1116,6 +1151,9 @@ struct OracleBVH {
 
 namespace {
 
+BBox def_bound(const OracleBVH* o) { return o->nodes[0].bounds; }  // definitions are not empty
+size_t def_size(const OracleBVH* o) { return o->R.prims.size(); }
+
 SplitMethod parse_split(const char* sm) {
     if (!sm) return SPLIT_SAH;
     if (!strcmp(sm, "sah")) return SPLIT_SAH;
@@ -1150,13 +1188,71 @@ int build_bvh(OracleBVH* o, uint32_t mp, SplitMethod sm) {
     return PBRT_OK;
 }
 
+// The aggregate of shapes with instance definitions: each definition
+// refined and built like the scene (the instance aggregate of
+// main.rs:745-753 with the scene's accelerator), then the shapes.
+int build_aggregate(const PbrtShapeDesc* shapes, uint32_t n, const PbrtInstanceDesc* defs, uint32_t n_defs,
+                    uint32_t mp, SplitMethod sm, OracleBVH* o) {
+    for (uint32_t k = 0; k < n_defs; ++k) {
+        auto d = std::make_shared<OracleBVH>();
+        for (uint32_t i = 0; i < defs[k].n_shapes; ++i)
+            if (defs[k].shapes[i].kind == PBRT_SHAPE_INSTANCE || defs[k].shapes[i].area_light >= 0) {
+                fprintf(stderr, "oracle: instance definitions hold neither instances nor area lights\n");
+                return PBRT_ERR_UNSUPPORTED;
+            }
+        if (!refine_shapes(defs[k].shapes, defs[k].n_shapes, &d->R)) {
+            fprintf(stderr, "oracle: %s\n", d->R.err.c_str());
+            return PBRT_ERR_INVALID_ARGUMENT;
+        }
+        if (d->R.prims.empty()) return PBRT_ERR_INVALID_ARGUMENT;
+        int st = build_bvh(d.get(), mp, sm);
+        if (st) return st;
+        o->R.defs.push_back(d);
+    }
+    if (!refine_shapes(shapes, n, &o->R)) {
+        fprintf(stderr, "oracle: %s\n", o->R.err.c_str());
+        return PBRT_ERR_INVALID_ARGUMENT;
+    }
+    if (!o->R.insts.empty()) {
+        uint64_t next = 0;
+        for (const Prim& p : o->R.prims) {
+            o->R.first_id.push_back((uint32_t)next);
+            next += p.kind == KIND_INST ? def_size(o->R.defs[o->R.insts[p.sphere].def].get()) : 1u;
+        }
+        if (next > 0x7fffffffull) return PBRT_ERR_UNSUPPORTED;
+    }
+    return build_bvh(o, mp, sm);
+}
+
 struct Counters {
     uint64_t nodes = 0, tris = 0, spheres = 0;
 };
 
+bool bvh_intersect_at(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo,
+                      int32_t* inner);
+
 // One primitive's intersect (geometric.rs:62-73): on a hit, shrinks maxt.
+// An instance (transformed.rs:35-56) traces the primitive-space ray
+// w2p(ray) - o as a point, d as a vector, mint and the current maxt kept -
+// through its definition's aggregate and, on a hit, takes its maxt; *inner
+// gets the definition-local refined index.
 bool prim_intersect(const Refined& R, const Prim& p, Ray& ray, float* t, float* b1, float* b2,
-                    Counters& C) {
+                    Counters& C, int32_t* inner) {
+    *inner = 0;
+    if (p.kind == KIND_INST) {
+        const Inst& I = R.insts[p.sphere];
+        Ray r = xf_ray(I.w2i, ray);
+        thread_local std::vector<uint32_t> todo2;
+        PbrtHit h;
+        int32_t unused;
+        if (!bvh_intersect_at(R.defs[I.def].get(), r, &h, C, todo2, &unused)) return false;
+        *t = h.t;
+        *b1 = h.b1;
+        *b2 = h.b2;
+        *inner = h.prim;
+        ray.maxt = r.maxt;
+        return true;
+    }
     if (p.kind == KIND_TRI) {
         C.tris++;
         if (!tri_hit(p.tri, ray, t, b1, b2)) return false;
@@ -1175,7 +1271,11 @@ bool prim_intersect(const Refined& R, const Prim& p, Ray& ray, float* t, float* 
 
 // bvh.rs:375-422.  BVH intersect_p is the default intersect().is_some()
 // (intersection.rs:61-66), so both use this full closest-hit search.
-bool bvh_intersect(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo) {
+// *compact gets the hit's refined index in this aggregate (hit->prim is
+// its id: with instances, the first id of the instance + the inner index).
+bool bvh_intersect_at(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo,
+                      int32_t* compact) {
+    *compact = -1;
     hit->prim = -1;
     hit->t = 0;
     hit->b1 = 0;
@@ -1201,8 +1301,10 @@ bool bvh_intersect(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std:
             for (uint32_t i = 0; i < node.count; ++i) {
                 uint32_t pi = o->ordered[node.offset + i];
                 float t, b1, b2;
-                if (prim_intersect(o->R, o->R.prims[pi], ray, &t, &b1, &b2, C)) {
-                    hit->prim = (int32_t)pi;
+                int32_t inner;
+                if (prim_intersect(o->R, o->R.prims[pi], ray, &t, &b1, &b2, C, &inner)) {
+                    *compact = (int32_t)pi;
+                    hit->prim = (int32_t)((o->R.first_id.empty() ? pi : o->R.first_id[pi]) + (uint32_t)inner);
                     hit->t = t;
                     hit->b1 = b1;
                     hit->b2 = b2;
@@ -1220,6 +1322,11 @@ bool bvh_intersect(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std:
         }
     }
     return any;
+}
+
+bool bvh_intersect(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo) {
+    int32_t compact;
+    return bvh_intersect_at(o, ray, hit, C, todo, &compact);
 }
 
 Ray to_ray(const PbrtRay& r) {
@@ -1502,9 +1609,8 @@ struct SceneData {
 };
 
 int scene_build(const PbrtSceneDesc* d, SceneData* S) {
-    if (!refine_shapes(d->shapes, d->n_shapes, &S->bvh.R)) return PBRT_ERR_INVALID_ARGUMENT;
     SplitMethod sm = (SplitMethod)d->split_method;
-    int st = build_bvh(&S->bvh, d->max_prims_in_node, sm);
+    int st = build_aggregate(d->shapes, d->n_shapes, d->instances, d->n_instances, d->max_prims_in_node, sm, &S->bvh);
     if (st) return st;
     S->materials.assign(d->materials, d->materials + d->n_materials);
     for (uint32_t i = 0; i < d->n_lights; ++i) {
@@ -1541,27 +1647,52 @@ struct SurfHit {
     V3 p, nn;
     float eps;
     int prim;
+    int material, area_light;
 };
+
+// dg.p and dg.nn of refined primitive p (a triangle or a quadric of R) hit
+// by ray r at t.
+void surface_dg(const Refined& R, const Prim& p, const Ray& r, float t, V3* pos, V3* nn) {
+    if (p.kind == KIND_TRI) {
+        tri_dg(p.tri, r, t, pos, nn, nullptr);
+        return;
+    }
+    const Sphere& s = R.spheres[p.sphere];
+    Ray orr = xf_ray(s.w2o.m, r);
+    float th, phi;
+    quad_hit_obj(s, orr, &th, &phi);  // recompute phi for u (same t)
+    if (s.kind == QUAD_SPHERE)
+        sphere_dg(s, orr, t, phi, pos, nn, nullptr, nullptr, nullptr, nullptr, nullptr);
+    else
+        quad_dg(s, orr, t, phi, pos, nn, nullptr, nullptr, nullptr, nullptr);
+}
 
 bool scene_intersect(const SceneData& S, const Ray& r_in, SurfHit* sh, Counters& C, std::vector<uint32_t>& todo) {
     Ray r = r_in;
     PbrtHit h;
-    if (!bvh_intersect(&S.bvh, r, &h, C, todo)) return false;
-    const Prim& p = S.bvh.R.prims[h.prim];
+    int32_t compact;
+    if (!bvh_intersect_at(&S.bvh, r, &h, C, todo, &compact)) return false;
+    const Refined& R = S.bvh.R;
+    const Prim& p = R.prims[compact];
     sh->prim = h.prim;
     sh->eps = h.t * 5e-4f;  // mesh.rs:262, sphere.rs:174
-    if (p.kind == KIND_TRI) {
-        tri_dg(p.tri, r_in, h.t, &sh->p, &sh->nn, nullptr);
+    if (p.kind == KIND_INST) {
+        // transformed.rs:37-51: the definition's primitive on the
+        // primitive-space ray, then p by primitive-to-world and nn by its
+        // normal transform, normalised
+        const Inst& I = R.insts[p.sphere];
+        const Refined& D = R.defs[I.def]->R;
+        const Prim& q = D.prims[(uint32_t)h.prim - R.first_id[compact]];
+        V3 pos, nn;
+        surface_dg(D, q, xf_ray(I.w2i, r_in), h.t, &pos, &nn);
+        sh->p = xf_point(I.i2w, pos);
+        sh->nn = normalize(xf_normal(I.w2i, nn));
+        sh->material = q.material;
+        sh->area_light = -1;
     } else {
-        const Sphere& s = S.bvh.R.spheres[p.sphere];
-        Ray orr = xf_ray(s.w2o.m, r_in);
-        orr.maxt = r_in.maxt;
-        float t, phi;
-        quad_hit_obj(s, orr, &t, &phi);  // recompute phi for u (same t)
-        if (s.kind == QUAD_SPHERE)
-            sphere_dg(s, orr, h.t, phi, &sh->p, &sh->nn, nullptr, nullptr, nullptr, nullptr, nullptr);
-        else
-            quad_dg(s, orr, h.t, phi, &sh->p, &sh->nn, nullptr, nullptr, nullptr, nullptr);
+        surface_dg(R, p, r_in, h.t, &sh->p, &sh->nn);
+        sh->material = p.material;
+        sh->area_light = p.area_light;
     }
     return true;
 }
@@ -1640,11 +1771,10 @@ void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, f
     L[0] = L[1] = L[2] = 0.0f;
     SurfHit h;
     if (!scene_intersect(S, ray, &h, C, todo)) return;  // miss: sum of le() is 0
-    const Prim& prim = S.bvh.R.prims[h.prim];
     V3 wo = neg(ray.d);
     // Le at an emitter (pbrt-v2 Intersection::Le; intersection.rs:58 is 0)
-    if (prim.area_light >= 0 && prim.area_light < (int)S.lights.size()) {
-        const Light& al = S.lights[prim.area_light];
+    if (h.area_light >= 0 && h.area_light < (int)S.lights.size()) {
+        const Light& al = S.lights[h.area_light];
         if (al.kind == PBRT_LIGHT_DIFFUSE_AREA && dot(h.nn, wo) > 0.0f) {
             const AreaLight& a = S.areas[al.area];
             L[0] = a.L[0];
@@ -1652,7 +1782,7 @@ void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, f
             L[2] = a.L[2];
         }
     }
-    const PbrtMaterialDesc& m = S.materials[prim.material];
+    const PbrtMaterialDesc& m = S.materials[h.material];
     float kd[3] = {clampf(m.kd[0], 0.0f, FLT_MAX), clampf(m.kd[1], 0.0f, FLT_MAX), clampf(m.kd[2], 0.0f, FLT_MAX)};
     float invpi = 1.0f / kPi;  // lambertian.rs:21
     size_t nl = S.lights.size();
@@ -1783,12 +1913,20 @@ extern "C" {
 int oracle_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t mp, const char* sm, OracleBVH** out) {
     if (!out || (!shapes && n_shapes)) return PBRT_ERR_INVALID_ARGUMENT;
     OracleBVH* o = new OracleBVH();
-    if (!refine_shapes(shapes, n_shapes, &o->R)) {
-        fprintf(stderr, "oracle: %s\n", o->R.err.c_str());
+    int st = build_aggregate(shapes, n_shapes, nullptr, 0, mp, parse_split(sm), o);
+    if (st) {
         delete o;
-        return PBRT_ERR_INVALID_ARGUMENT;
+        return st;
     }
-    int st = build_bvh(o, mp, parse_split(sm));
+    *out = o;
+    return PBRT_OK;
+}
+int oracle_bvh_create_desc(const PbrtSceneDesc* d, OracleBVH** out) {
+    if (!out || !d || (!d->shapes && d->n_shapes) || (!d->instances && d->n_instances))
+        return PBRT_ERR_INVALID_ARGUMENT;
+    OracleBVH* o = new OracleBVH();
+    int st = build_aggregate(d->shapes, d->n_shapes, d->instances, d->n_instances, d->max_prims_in_node,
+                             (SplitMethod)d->split_method, o);
     if (st) {
         delete o;
         return st;

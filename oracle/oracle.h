@@ -36,6 +36,9 @@ typedef struct OracleBVH OracleBVH;
 int oracle_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes,
                       uint32_t max_prims_in_node, const char* split_method,
                       OracleBVH** out);
+/* The aggregate of a scene description's shapes and instance definitions
+ * (TransformedPrimitive, src/primitive/transformed.rs:14-73). */
+int oracle_bvh_create_desc(const PbrtSceneDesc* desc, OracleBVH** out);
 void oracle_bvh_destroy(OracleBVH* bvh);
 int oracle_bvh_num_nodes(const OracleBVH* bvh, uint32_t* n);
 int oracle_bvh_num_primitives(const OracleBVH* bvh, uint32_t* n);

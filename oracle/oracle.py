@@ -35,6 +35,7 @@ def load() -> C.CDLL:
         sig = {
             "oracle_bvh_create": (C.c_int, [C.POINTER(abi.PbrtShapeDesc), C.c_uint32, C.c_uint32, C.c_char_p,
                                             C.POINTER(_P)]),
+            "oracle_bvh_create_desc": (C.c_int, [C.POINTER(abi.PbrtSceneDesc), C.POINTER(_P)]),
             "oracle_bvh_destroy": (None, [_P]),
             "oracle_bvh_num_nodes": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
             "oracle_bvh_num_primitives": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
@@ -104,8 +105,11 @@ class OracleBVH:
         prims = [p if isinstance(p, Primitive) else Primitive.simple(p) for p in prims]
         self.desc = SceneDescription(prims, [], max_prims, split_method, aggregate_only=True)
         h = C.c_void_p()
-        st = self.lib.oracle_bvh_create(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
-                                        split_method.encode(), C.byref(h))
+        if self.desc.definitions:  # instances (TransformedPrimitive) among the primitives
+            st = self.lib.oracle_bvh_create_desc(C.byref(self.desc.desc), C.byref(h))
+        else:
+            st = self.lib.oracle_bvh_create(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
+                                            split_method.encode(), C.byref(h))
         if st:
             raise abi.PbrtError(st, "oracle BVH build failed")
         self.h = h

@@ -21,10 +21,13 @@ STATUS_NAMES = {
     8: "PBRT_ERR_TIMEOUT", 9: "PBRT_ERR_NAN", 10: "PBRT_ERR_NO_DEVICE", 11: "PBRT_ERR_CANCELLED",
 }
 
+ABI_VERSION = 2  # PBRT_GPU_ABI_VERSION
+
 SHAPE_TRIANGLE_MESH = 0
 SHAPE_SPHERE = 1
 SHAPE_DISK = 2
 SHAPE_CYLINDER = 3
+SHAPE_INSTANCE = 4
 LIGHT_POINT = 0
 LIGHT_DIFFUSE_AREA = 1
 SPLIT_METHODS = {"sah": 0, "middle": 1, "equal": 2}
@@ -55,8 +58,13 @@ class PbrtShapeDesc(C.Structure):
         ("indices", C.POINTER(C.c_uint32)), ("n_indices", C.c_uint32),
         ("radius", C.c_float), ("z0", C.c_float), ("z1", C.c_float), ("phi_max_deg", C.c_float),
         ("height", C.c_float), ("inner_radius", C.c_float),
+        ("instance", C.c_int32),
         ("material", C.c_int32), ("area_light", C.c_int32),
     ]
+
+
+class PbrtInstanceDesc(C.Structure):
+    _fields_ = [("shapes", C.POINTER(PbrtShapeDesc)), ("n_shapes", C.c_uint32)]
 
 
 class PbrtMaterialDesc(C.Structure):
@@ -74,6 +82,7 @@ class PbrtSceneDesc(C.Structure):
         ("materials", C.POINTER(PbrtMaterialDesc)), ("n_materials", C.c_uint32),
         ("lights", C.POINTER(PbrtLightDesc)), ("n_lights", C.c_uint32),
         ("max_prims_in_node", C.c_uint32), ("split_method", C.c_int32), ("build_flags", C.c_uint32),
+        ("instances", C.POINTER(PbrtInstanceDesc)), ("n_instances", C.c_uint32),
     ]
 
 
@@ -158,6 +167,7 @@ SIGNATURES = {
                                      C.POINTER(_P)]),
     "pbrtgpu_bvh_create_ex": (C.c_int, [C.POINTER(PbrtShapeDesc), C.c_uint32, C.c_uint32, C.c_char_p, C.c_uint32,
                                         C.POINTER(C.c_void_p)]),
+    "pbrtgpu_bvh_create_desc": (C.c_int, [C.POINTER(PbrtSceneDesc), C.POINTER(C.c_void_p)]),
     "pbrtgpu_bvh_destroy": (None, [_P]),
     "pbrtgpu_bvh_world_bound": (C.c_int, [_P, _F3, _F3]),
     "pbrtgpu_bvh_num_primitives": (C.c_int, [_P, _U32P]),
@@ -222,7 +232,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.pbrtgpu_abi_version() != 1:
+    if lib.pbrtgpu_abi_version() != ABI_VERSION:
         raise RuntimeError("pbrt_gpu ABI version mismatch")
     if path is None:
         _lib = lib

@@ -21,7 +21,8 @@ WorldBegin/WorldEnd, AttributeBegin/End, TransformBegin/End,
 ReverseOrientation, Material / MakeNamedMaterial / NamedMaterial "matte",
 Texture "constant", LightSource "point", AreaLightSource "diffuse" on
 triangle meshes, Shape "sphere", "disk", "cylinder" and "trianglemesh", ObjectBegin/End and
-ObjectInstance (flattened into the scene, see ``object_instance``), Include.
+ObjectInstance (TransformedPrimitive instances sharing one BVH per
+definition, see ``object_instance``), Include.
 Anything else raises ``NotImplementedError`` (the reference panics).
 """
 from __future__ import annotations
@@ -33,8 +34,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .scene import (Camera, DiffuseAreaLight, Film, Filter, MatteMaterial, PointLight, Primitive, Shape,
-                    StratifiedSampler, default_num_tasks)
+from .scene import (Camera, DiffuseAreaLight, Film, Filter, InstanceDefinition, MatteMaterial, PointLight,
+                    Primitive, Shape, StratifiedSampler, default_num_tasks)
 from .transform import Transform
 
 
@@ -291,6 +292,7 @@ class Pbrt:
         self.lights: list = []
         self.primitives: list = []
         self.instances: dict[str, list] = {}
+        self.definitions: dict[str, InstanceDefinition] = {}  # shared by the instances of a name
         self.current_instance: str | None = None
 
     def _verify(self, want: int, what: str):
@@ -496,6 +498,7 @@ class Pbrt:
         if self.current_instance is not None:
             raise RuntimeError("ObjectBegin called inside of instance definition")
         self.instances[name] = []
+        self.definitions.pop(name, None)
         self.current_instance = name
 
     def object_end(self):
@@ -506,19 +509,29 @@ class Pbrt:
         self.attribute_end()
 
     def object_instance(self, name):
-        """The instance's shapes placed by the current transform, as
-        pbrt-v2's TransformedPrimitive places them (the reference computes
-        the transform but pushes the untransformed primitive and cannot
-        build the instance aggregate, main.rs:735-763).  The device has no
-        two-level traversal, so each shape is copied with its
-        object-to-world transform composed with the instance's."""
+        """ObjectInstance (main.rs:735-763) placed as pbrt-v2 places it: a
+        TransformedPrimitive (transformed.rs:14-59) over the definition's
+        aggregate, its world-to-primitive transform the inverse of the
+        current transform (the reference computes that transform but pushes
+        the untransformed primitive, and cannot build the aggregate).  All
+        instances of a definition share one device BVH.  A definition that
+        holds area lights is copied out instead, shape by shape with the
+        composed transform, since an emitter is sampled in world space."""
         self._verify(STATE_WORLD_BLOCK, "ObjectInstance")
         if name not in self.instances:
             print(f"Can't find object named {name}")
             return
+        if not self.instances[name]:  # main.rs:741-743
+            return
         if self.ctm[0] != self.ctm[1]:
             raise NotImplementedError("animated instances are not rendered on the device")
         inst = self.ctm[0]
+        if all(p.area_light is None for p in self.instances[name]):
+            defn = self.definitions.get(name)
+            if defn is None:
+                defn = self.definitions[name] = InstanceDefinition(list(self.instances[name]))
+            self.primitives.append(Primitive.transformed(defn, inst.inverse()))
+            return
         for p in self.instances[name]:
             s = p.shape
             moved = dataclasses.replace(s, object_to_world=inst * s.object_to_world)

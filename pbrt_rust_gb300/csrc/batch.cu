@@ -20,7 +20,7 @@
 
 namespace pbrt {
 
-cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed,
+cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool inst,
                                uint32_t cover_pair, uint32_t cover_wide, int sms, cudaStream_t s);
 
 namespace {
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(BLOCK) kb_film(BatchArgs A) {
 
 }  // namespace
 
-cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool mixed, uint32_t cover_pair,
+cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool mixed, bool inst, uint32_t cover_pair,
                                 uint32_t cover_wide, int sms, size_t counter_bytes, cudaStream_t s, int* launches) {
     *launches = 0;
     cudaError_t e = cudaMemsetAsync(A.counters, 0, counter_bytes, s);
@@ -111,10 +111,10 @@ cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool m
     };
     const bool b256 = T.block == 256;
     if ((e = b256 ? stage(kb_generate<256>) : stage(kb_generate<128>)) != cudaSuccess) return e;
-    if ((e = launch_batch_trace(A, T, false, mixed, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;
+    if ((e = launch_batch_trace(A, T, false, mixed, inst, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;
     ++*launches;
     if ((e = b256 ? stage(kb_shade<256>) : stage(kb_shade<128>)) != cudaSuccess) return e;
-    if ((e = launch_batch_trace(A, T, true, false, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;
+    if ((e = launch_batch_trace(A, T, true, false, inst, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;
     ++*launches;
     if ((e = b256 ? stage(kb_combine<256>) : stage(kb_combine<128>)) != cudaSuccess) return e;
     if ((e = b256 ? stage(kb_film<256>) : stage(kb_film<128>)) != cudaSuccess) return e;

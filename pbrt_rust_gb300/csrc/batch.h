@@ -75,11 +75,13 @@ struct BatchTuning {
 
 // Enqueues every stage of the batch on `s`, starting with zeroing the
 // counter_bytes of A.counters.  mixed: some query job wants any hit (the
-// extend kernel then decides per job).  cover_pair / cover_wide: the stack
-// size the jobs need (64 or 256 entries).  *launches gets the number of
+// extend kernel then decides per job).  inst: some job's scene has
+// instances (the binary layout with nested instance traversal is used).
+// cover_pair / cover_wide: the stack size the jobs need (64 or 256
+// entries).  *launches gets the number of
 // kernels launched.  A traversal failure of job j goes to
 // jobs[j].P.counters[2] (PbrtStatus, max over its rays).
-cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool mixed, uint32_t cover_pair,
+cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool mixed, bool inst, uint32_t cover_pair,
                                 uint32_t cover_wide, int sms, size_t counter_bytes, cudaStream_t s, int* launches);
 
 }  // namespace pbrt

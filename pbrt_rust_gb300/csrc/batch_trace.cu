@@ -91,9 +91,10 @@ struct Walker<true, SMAX, OVF> {
     __device__ __forceinline__ const TraceResult& res() const { return T.res; }
 };
 
-template <int STACK, int UNUSED>
-struct Walker<false, STACK, UNUSED> {
-    Traversal<STACK> T;
+// INST = 1: the tree may hold instances (Traversal with INST).
+template <int STACK, int INST>
+struct Walker<false, STACK, INST> {
+    Traversal<STACK, INST != 0> T;
     DevBVH bv;
     int st = 0;
     __device__ __forceinline__ void bind(uint2*) {}
@@ -193,7 +194,9 @@ cudaError_t go(const BatchArgs& A, int sms, cudaStream_t s) {
 }
 
 template <int BLOCK, bool SHADOW, int MODE>
-cudaError_t pick(const BatchArgs& A, const BatchTuning& T, bool wide, uint32_t cover, int sms, cudaStream_t s) {
+cudaError_t pick(const BatchArgs& A, const BatchTuning& T, bool wide, bool inst, uint32_t cover, int sms,
+                 cudaStream_t s) {
+    if (inst) return go<BLOCK, SHADOW, false, 256, 1, MODE>(A, sms, s);
     if (wide) {
         if (T.smax == 8)
             return cover <= 64 ? go<BLOCK, SHADOW, true, 8, 56, MODE>(A, sms, s)
@@ -206,22 +209,22 @@ cudaError_t pick(const BatchArgs& A, const BatchTuning& T, bool wide, uint32_t c
 }
 
 template <int BLOCK>
-cudaError_t pick_block(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool wide, uint32_t cover,
-                       int sms, cudaStream_t s) {
-    if (shadow) return pick<BLOCK, true, kAny>(A, T, wide, cover, sms, s);
-    return mixed ? pick<BLOCK, false, kPerJob>(A, T, wide, cover, sms, s)
-                 : pick<BLOCK, false, kClosest>(A, T, wide, cover, sms, s);
+cudaError_t pick_block(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool wide, bool inst,
+                       uint32_t cover, int sms, cudaStream_t s) {
+    if (shadow) return pick<BLOCK, true, kAny>(A, T, wide, inst, cover, sms, s);
+    return mixed ? pick<BLOCK, false, kPerJob>(A, T, wide, inst, cover, sms, s)
+                 : pick<BLOCK, false, kClosest>(A, T, wide, inst, cover, sms, s);
 }
 
 }  // namespace
 
-cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed,
+cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool inst,
                                uint32_t cover_pair, uint32_t cover_wide, int sms, cudaStream_t s) {
-    const bool wide = shadow ? T.shadow_wide : T.extend_wide;
+    const bool wide = !inst && (shadow ? T.shadow_wide : T.extend_wide);
     const uint32_t cover = wide ? cover_wide : cover_pair;
     if (cover > 256) return cudaErrorInvalidValue;
-    if (T.block == 256) return pick_block<256>(A, T, shadow, mixed, wide, cover, sms, s);
-    return pick_block<128>(A, T, shadow, mixed, wide, cover, sms, s);
+    if (T.block == 256) return pick_block<256>(A, T, shadow, mixed, wide, inst, cover, sms, s);
+    return pick_block<128>(A, T, shadow, mixed, wide, inst, cover, sms, s);
 }
 
 }  // namespace pbrt

@@ -100,6 +100,33 @@ int bvh_upload(PbrtBVH* b) {
     if ((st = upload(&b->d_nodes4, b->host.nodes4))) return st;
     if ((st = cuda_status(cudaMalloc(&b->d_status, sizeof(int)), "cudaMalloc"))) return st;
     if ((st = cuda_status(cudaMemset(b->d_status, 0, sizeof(int)), "cudaMemset"))) return st;
+    // instance definitions: binary layout, traced by instance_test
+    std::vector<DevBVH> defs;
+    for (const HostBVH& I : b->host.insts) {
+        NodePair* pairs = nullptr;
+        PrimRec* prims = nullptr;
+        SphereRec* spheres = nullptr;
+        st = upload(&pairs, I.pairs);
+        if (pairs) b->d_inst_bufs.push_back(pairs);
+        if (!st) st = upload(&prims, I.recs);
+        if (prims) b->d_inst_bufs.push_back(prims);
+        if (!st) st = upload(&spheres, I.spheres);
+        if (spheres) b->d_inst_bufs.push_back(spheres);
+        if (st) return st;
+        DevBVH d{};
+        d.pairs = pairs;
+        d.prims = prims;
+        d.spheres = spheres;
+        d.root = I.root;
+        d.has_spheres = I.has_spheres ? 1u : 0u;
+        d.n_prims = (uint32_t)I.recs.size();
+        d.empty = I.nodes.empty() ? 1u : 0u;
+        d.insts = nullptr;
+        defs.push_back(d);
+    }
+    b->inst_dev = defs;
+    if ((st = upload(&b->d_insts, defs))) return st;
+    b->dev.insts = b->d_insts;
     b->dev.pairs = b->d_pairs;
     b->dev.prims = b->d_prims;
     b->dev.spheres = b->d_spheres;
@@ -116,8 +143,10 @@ int bvh_upload(PbrtBVH* b) {
     return PBRT_OK;
 }
 
-// The 4-wide layout when a compiled variant covers its stack bound.
+// The 4-wide layout when a compiled variant covers its stack bound (never
+// for a tree with instances: those take the binary walk).
 const DevBVH4* wide_of(const PbrtBVH* b) {
+    if (!b->host.insts.empty()) return nullptr;
     return wide_stack_variant(b->host.stack4_bound) ? &b->dev4 : nullptr;
 }
 
@@ -250,6 +279,8 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
 }  // namespace pbrt
 
 PbrtBVH::~PbrtBVH() {
+    for (void* p : d_inst_bufs) cudaFree(p);
+    if (d_insts) cudaFree(d_insts);
     if (d_pairs) cudaFree(d_pairs);
     if (d_prims) cudaFree(d_prims);
     if (d_spheres) cudaFree(d_spheres);
@@ -288,16 +319,18 @@ int pbrtgpu_bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t 
     return pbrtgpu_bvh_create_ex(shapes, n_shapes, max_prims, split_method, 0, out);
 }
 
-int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims,
-                          const char* split_method, uint32_t flags, PbrtBVH** out) {
-    if (!out || (!shapes && n_shapes)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+static int bvh_create(const PbrtShapeDesc* shapes, uint32_t n_shapes, const PbrtInstanceDesc* defs, uint32_t n_defs,
+                      uint32_t max_prims, const char* split_method, uint32_t flags, PbrtBVH** out) {
+    if (!out || (!shapes && n_shapes) || (!defs && n_defs)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
+    for (uint32_t k = 0; k < n_defs; ++k)
+        if (!defs[k].shapes && defs[k].n_shapes) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (flags & ~(uint32_t)PBRT_BUILD_ON_DEVICE) return set_error(PBRT_ERR_INVALID_ARGUMENT, "unknown build flags");
     const bool on_device = (flags & PBRT_BUILD_ON_DEVICE) != 0;
     if (on_device && !cuda_device_present()) return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device for the build");
     PbrtBVH* b = new PbrtBVH();
     std::string err;
-    int st = build_host_bvh(shapes, n_shapes, max_prims, split_method, &b->host, &err, on_device);
+    int st = build_host_bvh(shapes, n_shapes, max_prims, split_method, &b->host, &err, on_device, defs, n_defs);
     if (st) {
         delete b;
         return set_error(st, err);
@@ -315,6 +348,19 @@ int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32
     }
     *out = b;
     return PBRT_OK;
+}
+
+int pbrtgpu_bvh_create_ex(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims,
+                          const char* split_method, uint32_t flags, PbrtBVH** out) {
+    return bvh_create(shapes, n_shapes, nullptr, 0, max_prims, split_method, flags, out);
+}
+
+int pbrtgpu_bvh_create_desc(const PbrtSceneDesc* d, PbrtBVH** out) {
+    if (!d) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    const char* names[3] = {"sah", "middle", "equal"};
+    const char* sm = (d->split_method >= 0 && d->split_method < 3) ? names[d->split_method] : "sah";
+    return bvh_create(d->shapes, d->n_shapes, d->instances, d->n_instances, d->max_prims_in_node, sm, d->build_flags,
+                      out);
 }
 
 void pbrtgpu_bvh_destroy(PbrtBVH* b) {

@@ -111,7 +111,7 @@ struct PbrtBatch {
     uint32_t n_jobs = 0;
     uint64_t n_pix = 0, n_ray = 0, n_smp = 0, n_lsmp = 0, n_film = 0, n_tasks = 0, n_stage = 0;
     uint32_t cover_pair = 64, cover_wide = 64;
-    bool all_wide = true, mixed = false;
+    bool all_wide = true, mixed = false, inst = false;
     std::vector<Copy> h2d, d2h;  // staged host inputs / outputs of the jobs
     bool in_flight = false;
 
@@ -120,6 +120,7 @@ struct PbrtBatch {
     cudaGraphExec_t graph = nullptr;
     BatchTuning graph_tune{};
     bool graph_mixed = false;
+    bool graph_inst = false;
     uint32_t graph_cover_pair = 0, graph_cover_wide = 0;
     int graph_kernels = 0;
     int last_kernels = 0;
@@ -172,6 +173,7 @@ struct PbrtBatch {
         cover_pair = cover_wide = 64;
         all_wide = true;
         mixed = false;
+        inst = false;
         h2d.clear();
         d2h.clear();
         uint64_t* offs[4] = {off(lay.o_pix), off(lay.o_ray), off(lay.o_smp), off(lay.o_film)};
@@ -195,7 +197,8 @@ namespace {
 int enqueue_stages(PbrtBatch* b, cudaStream_t s) {
     BatchArgs A = b->args();
     const bool key_match = b->graph && !std::memcmp(&b->graph_tune, &b->tune, sizeof(BatchTuning)) &&
-                           b->graph_mixed == b->mixed && b->graph_cover_pair == b->cover_pair &&
+                           b->graph_mixed == b->mixed && b->graph_inst == b->inst &&
+                           b->graph_cover_pair == b->cover_pair &&
                            b->graph_cover_wide == b->cover_wide;
     // the graph zeroes every job slot's counters, so it serves any job count
     const size_t cbytes = (size_t)(b->lim.max_jobs + 1) * kCtrWords * 4;
@@ -205,7 +208,7 @@ int enqueue_stages(PbrtBatch* b, cudaStream_t s) {
         return cuda_status(cudaGraphLaunch(b->graph, s), "cudaGraphLaunch");
     }
     int n = 0;
-    int st = cuda_status(launch_batch_stages(A, b->tune, b->mixed, b->cover_pair, b->cover_wide, b->sms, cbytes, s, &n),
+    int st = cuda_status(launch_batch_stages(A, b->tune, b->mixed, b->inst, b->cover_pair, b->cover_wide, b->sms, cbytes, s, &n),
                          "batch stages");
     if (st) return st;
     b->last_graph = false;
@@ -221,7 +224,8 @@ int enqueue_stages(PbrtBatch* b, cudaStream_t s) {
             return st;
         int m = 0;
         cudaError_t e =
-            launch_batch_stages(A, b->tune, b->mixed, b->cover_pair, b->cover_wide, b->sms, cbytes, b->cap_stream, &m);
+            launch_batch_stages(A, b->tune, b->mixed, b->inst, b->cover_pair, b->cover_wide, b->sms, cbytes,
+                                b->cap_stream, &m);
         cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &g);
         if (e == cudaSuccess) e = e2;
         if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -232,6 +236,7 @@ int enqueue_stages(PbrtBatch* b, cudaStream_t s) {
         }
         b->graph_tune = b->tune;
         b->graph_mixed = b->mixed;
+        b->graph_inst = b->inst;
         b->graph_cover_pair = b->cover_pair;
         b->graph_cover_wide = b->cover_wide;
         b->graph_kernels = m;
@@ -377,7 +382,8 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
                                           "samples, film pixels or tasks");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(P.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
-    const uint32_t cw = P.has_wide ? (uint32_t)wide_stack_variant(P.wide_bound) : 0u;
+    const bool inst = P.bvh.insts != nullptr;  // instances: binary layout only
+    const uint32_t cw = (P.has_wide && !inst) ? (uint32_t)wide_stack_variant(P.wide_bound) : 0u;
     const uint32_t j = b->n_jobs;
     const Layout& Y = b->lay;
     float* table = reinterpret_cast<float*>(b->h + Y.o_tables) + (size_t)j * 256;
@@ -416,6 +422,7 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
     b->n_lsmp += SL;
     b->n_film += npx;
     b->cover_pair = std::max(b->cover_pair, cp);
+    b->inst = b->inst || inst;
     if (cw)
         b->cover_wide = std::max(b->cover_wide, cw);
     else
@@ -444,7 +451,8 @@ int pbrtgpu_batch_add_query(PbrtBatch* b, const PbrtBVH* cb, const PbrtRay* rays
         return set_error(PBRT_ERR_BUDGET, "the query does not fit the batch's remaining jobs or staged rays");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(B->host.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
-    const DevBVH4* w = wide_of(B);
+    const bool inst = B->dev.insts != nullptr;  // instances: binary layout only
+    const DevBVH4* w = inst ? nullptr : wide_of(B);
     const uint32_t cw = w ? (uint32_t)wide_stack_variant(B->host.stack4_bound) : 0u;
     const uint32_t j = b->n_jobs;
     const Layout& Y = b->lay;
@@ -477,6 +485,7 @@ int pbrtgpu_batch_add_query(PbrtBatch* b, const PbrtBVH* cb, const PbrtRay* rays
     if (staged) b->n_stage += n;
     b->n_ray += n;
     b->cover_pair = std::max(b->cover_pair, cp);
+    b->inst = b->inst || inst;
     if (cw)
         b->cover_wide = std::max(b->cover_wide, cw);
     else

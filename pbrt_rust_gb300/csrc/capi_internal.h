@@ -44,6 +44,9 @@ struct PbrtBVH {
     pbrt::PrimRec* d_prims = nullptr;
     pbrt::SphereRec* d_spheres = nullptr;
     pbrt::Node4* d_nodes4 = nullptr;
+    pbrt::DevBVH* d_insts = nullptr;     // per instance definition
+    std::vector<void*> d_inst_bufs;      // the definitions' device arrays
+    std::vector<pbrt::DevBVH> inst_dev;  // host copy of d_insts
     int* d_status = nullptr;
     pbrt::DevBVH dev{};
     pbrt::DevBVH4 dev4{};
@@ -66,6 +69,11 @@ struct PbrtScene {
     std::vector<pbrt::LightRec> lights;
     std::vector<pbrt::AreaTri> area_tris;
     std::vector<float> area_cdf;
+    std::vector<std::vector<pbrt::ShadePrim>> inst_shade;  // per instance definition
+    std::vector<uint4> inst_map;                           // RenderParams::inst_map
+    std::vector<void*> d_inst_bufs;
+    uint4* d_inst_map = nullptr;
+    pbrt::InstShade* d_inst_defs = nullptr;
     pbrt::ShadePrim* d_shade = nullptr;
     float4* d_materials = nullptr;
     pbrt::LightRec* d_lights = nullptr;
@@ -76,8 +84,10 @@ struct PbrtScene {
     pbrt::DeviceBuf rays, hits, img, pixbox, lsamp, contrib, le, L, srays, sslot, occ, counters, tasks, table, rgb;
     ~PbrtScene() {
         if (bvh) delete bvh;
-        for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lights, (void*)d_area_tris, (void*)d_area_cdf})
+        for (void* p : {(void*)d_shade, (void*)d_materials, (void*)d_lights, (void*)d_area_tris, (void*)d_area_cdf,
+                        (void*)d_inst_map, (void*)d_inst_defs})
             if (p) cudaFree(p);
+        for (void* p : d_inst_bufs) cudaFree(p);
         for (pbrt::DeviceBuf* b : {&rays, &hits, &img, &pixbox, &lsamp, &contrib, &le, &L, &srays, &sslot, &occ, &counters,
                                    &tasks, &table, &rgb})
             b->release();

@@ -209,6 +209,9 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     P.n_lights = nl;
     P.area_tris = S->d_area_tris;
     P.area_cdf = S->d_area_cdf;
+    P.n_inst = (uint32_t)S->inst_map.size();
+    P.inst_map = S->d_inst_map;
+    P.inst_defs = S->d_inst_defs;
     P.rays = (PbrtRay*)p_rays;
     P.hits = (float4*)p_hits;
     P.img = (float2*)p_img;

@@ -149,6 +149,16 @@ static int scene_upload(PbrtScene* S) {
     if ((st = up(&S->d_lights, S->lights))) return st;
     if ((st = up(&S->d_area_tris, S->area_tris))) return st;
     if ((st = up(&S->d_area_cdf, S->area_cdf))) return st;
+    if ((st = up(&S->d_inst_map, S->inst_map))) return st;
+    std::vector<InstShade> defs;
+    for (size_t k = 0; k < S->inst_shade.size(); ++k) {
+        ShadePrim* sh = nullptr;
+        st = up(&sh, S->inst_shade[k]);
+        if (sh) S->d_inst_bufs.push_back(sh);
+        if (st) return st;
+        defs.push_back(InstShade{sh, S->bvh->inst_dev[k].spheres});
+    }
+    if ((st = up(&S->d_inst_defs, defs))) return st;
     S->uploaded = true;
     return PBRT_OK;
 }
@@ -164,6 +174,30 @@ static inline float bitsf(uint32_t u) {
     return f;
 }
 
+// Per refined primitive shading records (ShadePrim) of one BVH.
+static void shade_records(const HostBVH& H, std::vector<ShadePrim>* out) {
+    out->resize(H.prims.size());
+    for (size_t i = 0; i < H.prims.size(); ++i) {
+        const HostPrim& p = H.prims[i];
+        ShadePrim& r = (*out)[i];
+        std::memset(&r, 0, sizeof(r));
+        r.a[0] = p.p1.x;
+        r.a[1] = p.p1.y;
+        r.a[2] = p.p1.z;
+        r.a[3] = bitsf((uint32_t)p.material);
+        r.b[0] = p.p2.x;
+        r.b[1] = p.p2.y;
+        r.b[2] = p.p2.z;
+        r.b[3] = bitsf(p.area_light >= 0 ? (uint32_t)p.area_light + 1u : 0u);
+        r.c[0] = p.p3.x;
+        r.c[1] = p.p3.y;
+        r.c[2] = p.p3.z;
+        uint32_t flags = (p.flip ? kShadeFlip : 0u);
+        if (p.kind == PBRT_SHAPE_SPHERE) flags |= kShadeSphere | ((uint32_t)p.sphere << 2);
+        r.c[3] = bitsf(flags);
+    }
+}
+
 }  // namespace pbrt
 
 extern "C" {
@@ -173,8 +207,23 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
         (!d->materials && d->n_materials))
         return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
+    if (!d->instances && d->n_instances) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (uint32_t k = 0; k < d->n_instances; ++k) {
+        const PbrtInstanceDesc& D = d->instances[k];
+        if (!D.shapes && D.n_shapes) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+        for (uint32_t i = 0; i < D.n_shapes; ++i)
+            if (D.shapes[i].kind != PBRT_SHAPE_INSTANCE &&
+                (D.shapes[i].material < 0 || (uint32_t)D.shapes[i].material >= d->n_materials))
+                return set_error(PBRT_ERR_INVALID_ARGUMENT, "instance definition " + std::to_string(k) + " shape " +
+                                                                std::to_string(i) + ": material index out of range");
+    }
     for (uint32_t i = 0; i < d->n_shapes; ++i) {
         const PbrtShapeDesc& sd = d->shapes[i];
+        if (sd.kind == PBRT_SHAPE_INSTANCE) {  // its definition's shapes carry the materials
+            if (sd.area_light >= 0)
+                return set_error(PBRT_ERR_UNSUPPORTED, "shape " + std::to_string(i) + ": area light on an instance");
+            continue;
+        }
         if (sd.material < 0 || (uint32_t)sd.material >= d->n_materials)
             return set_error(PBRT_ERR_INVALID_ARGUMENT, "shape " + std::to_string(i) + ": material index out of range");
         if (sd.area_light >= 0) {
@@ -201,7 +250,8 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
         delete S;
         return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device for the build");
     }
-    int st = build_host_bvh(d->shapes, d->n_shapes, d->max_prims_in_node, sm, &S->bvh->host, &err, on_device);
+    int st = build_host_bvh(d->shapes, d->n_shapes, d->max_prims_in_node, sm, &S->bvh->host, &err, on_device,
+                            d->instances, d->n_instances);
     if (st) {
         delete S;
         return set_error(st, err);
@@ -211,26 +261,14 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
         return set_error(PBRT_ERR_STACK_OVERFLOW, "BVH too deep for the traversal stack");
     }
     const HostBVH& H = S->bvh->host;
-    // per refined primitive shading records
-    S->shade.resize(H.prims.size());
+    shade_records(H, &S->shade);
+    S->inst_shade.resize(H.insts.size());
+    for (size_t k = 0; k < H.insts.size(); ++k) shade_records(H.insts[k], &S->inst_shade[k]);
     for (size_t i = 0; i < H.prims.size(); ++i) {
         const HostPrim& p = H.prims[i];
-        ShadePrim& r = S->shade[i];
-        std::memset(&r, 0, sizeof(r));
-        r.a[0] = p.p1.x;
-        r.a[1] = p.p1.y;
-        r.a[2] = p.p1.z;
-        r.a[3] = bitsf((uint32_t)p.material);
-        r.b[0] = p.p2.x;
-        r.b[1] = p.p2.y;
-        r.b[2] = p.p2.z;
-        r.b[3] = bitsf(p.area_light >= 0 ? (uint32_t)p.area_light + 1u : 0u);
-        r.c[0] = p.p3.x;
-        r.c[1] = p.p3.y;
-        r.c[2] = p.p3.z;
-        uint32_t flags = (p.flip ? kShadeFlip : 0u);
-        if (p.kind == PBRT_SHAPE_SPHERE) flags |= kShadeSphere | ((uint32_t)p.sphere << 2);
-        r.c[3] = bitsf(flags);
+        if (p.sphere < 0 || H.spheres[p.sphere].kind != kQuadInstance) continue;
+        const uint32_t n_inner = (uint32_t)H.insts[H.spheres[p.sphere].instance].prims.size();
+        S->inst_map.push_back(make_uint4(H.flat_id[i], (uint32_t)i, n_inner, (uint32_t)p.sphere));
     }
     // matte Kd clamped to [0, f32::MAX] (matte.rs:42)
     for (uint32_t i = 0; i < d->n_materials; ++i) {
@@ -434,6 +472,9 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
     P.n_lights = nl;
     P.area_tris = S->d_area_tris;
     P.area_cdf = S->d_area_cdf;
+    P.n_inst = (uint32_t)S->inst_map.size();
+    P.inst_map = S->d_inst_map;
+    P.inst_defs = S->d_inst_defs;
     *out = P;
     *tasks_out = std::move(tasks);
     return PBRT_OK;

@@ -251,7 +251,13 @@ void prim_bounds(const HostBVH& H, std::vector<Box>* bounds, std::vector<float>*
             const SphereRec& s = H.spheres[p.sphere];
             M4 o2w;
             std::memcpy(o2w.m, s.o2w, sizeof(o2w.m));
-            b = xf_box(o2w, Box{v3(-s.radius, -s.radius, s.z_min), v3(s.radius, s.radius, s.z_max)});
+            if (s.kind == kQuadInstance) {
+                // transformed.rs:62-65: motion_bounds of a static transform =
+                // the definition's bound through primitive-to-world
+                b = xf_box(o2w, H.insts[s.instance].nodes[0].box);  // definitions are not empty
+            } else {
+                b = xf_box(o2w, Box{v3(-s.radius, -s.radius, s.z_min), v3(s.radius, s.radius, s.z_max)});
+            }
         }
         (*bounds)[i] = b;
         V3 c = (b.lo + b.hi) * 0.5f;  // bvh.rs:77
@@ -424,7 +430,7 @@ static void fill_device_layout(HostBVH& H) {
         const HostPrim& p = H.prims[H.ordered[i]];
         PrimRec& r = H.recs[i];
         std::memset(&r, 0, sizeof(r));
-        uint32_t id = H.ordered[i];
+        uint32_t id = H.flat_id.empty() ? H.ordered[i] : H.flat_id[H.ordered[i]];
         if (p.kind == PBRT_SHAPE_TRIANGLE_MESH) {
             V3 e1 = p.p2 - p.p1, e2 = p.p3 - p.p1;  // mesh.rs:45-46
             r.r0[0] = p.p1.x;
@@ -531,9 +537,30 @@ static void fill_node4_layout(HostBVH& H) {
 }
 
 int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
-                   HostBVH* out, std::string* err, bool on_device) {
+                   HostBVH* out, std::string* err, bool on_device, const PbrtInstanceDesc* defs, uint32_t n_defs) {
     HostBVH& H = *out;
     H = HostBVH();
+    // the definitions' BVHs, built like the scene's (the instance aggregate
+    // of ObjectInstance uses the scene's accelerator, main.rs:735-763)
+    H.insts.resize(n_defs);
+    for (uint32_t k = 0; k < n_defs; ++k) {
+        for (uint32_t i = 0; i < defs[k].n_shapes; ++i)
+            if (defs[k].shapes[i].kind == PBRT_SHAPE_INSTANCE || defs[k].shapes[i].area_light >= 0) {
+                *err = "instance definitions hold neither instances nor area lights";
+                return PBRT_ERR_UNSUPPORTED;
+            }
+        int st = build_host_bvh(defs[k].shapes, defs[k].n_shapes, max_prims, split_method, &H.insts[k], err,
+                                on_device);
+        if (st) return st;
+        if (H.insts[k].prims.empty()) {
+            *err = "instance definition without shapes";
+            return PBRT_ERR_INVALID_ARGUMENT;
+        }
+        if (H.insts[k].depth > 64) {
+            *err = "instance definition BVH deeper than 64 levels";
+            return PBRT_ERR_UNSUPPORTED;
+        }
+    }
     // Full refinement: primitive/mod.rs:47-63, mesh.rs:298-338.
     for (uint32_t si = 0; si < n_shapes; ++si) {
         const PbrtShapeDesc& d = shapes[si];
@@ -597,6 +624,26 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
             H.spheres.push_back(s);
             H.prims.push_back(p);
             H.has_spheres = true;
+        } else if (d.kind == PBRT_SHAPE_INSTANCE) {
+            if (d.instance < 0 || (uint32_t)d.instance >= n_defs) {
+                *err = "instance: definition index out of range";
+                return PBRT_ERR_INVALID_ARGUMENT;
+            }
+            SphereRec s{};
+            std::memcpy(s.o2w, o2w.m.m, sizeof(s.o2w));   // primitive to world
+            std::memcpy(s.w2o, o2w.mi.m, sizeof(s.w2o));  // world to primitive
+            s.kind = kQuadInstance;
+            s.instance = (uint32_t)d.instance;
+            HostPrim p{};
+            p.kind = PBRT_SHAPE_SPHERE;  // one analytic-style primitive
+            p.shape = (int)si;
+            p.material = d.material;
+            p.area_light = -1;
+            p.flip = false;
+            p.sphere = (int)H.spheres.size();
+            H.spheres.push_back(s);
+            H.prims.push_back(p);
+            H.has_spheres = true;
         } else if (d.kind == PBRT_SHAPE_DISK || d.kind == PBRT_SHAPE_CYLINDER) {
             SphereRec s{};
             std::memcpy(s.o2w, o2w.m.m, sizeof(s.o2w));
@@ -631,6 +678,25 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
             *err = "unknown shape kind";
             return PBRT_ERR_INVALID_ARGUMENT;
         }
+    }
+    bool any_instance = false;
+    for (const SphereRec& s : H.spheres) any_instance |= s.kind == kQuadInstance;
+    if (any_instance) {
+        H.flat_id.resize(H.prims.size());
+        uint64_t next = 0;
+        for (size_t i = 0; i < H.prims.size(); ++i) {
+            H.flat_id[i] = (uint32_t)next;
+            const HostPrim& p = H.prims[i];
+            const bool inst = p.sphere >= 0 && H.spheres[p.sphere].kind == kQuadInstance;
+            next += inst ? H.insts[H.spheres[p.sphere].instance].prims.size() : 1u;
+            if (next > 0x7fffffffull) {
+                *err = "more than 2^31 - 1 primitives with the instances counted out";
+                return PBRT_ERR_UNSUPPORTED;
+            }
+        }
+        H.n_flat = next;
+    } else {
+        H.n_flat = H.prims.size();
     }
     const int split = parse_split_method(split_method);
     // equal-counts splits of large ranges use the sequential partition_by

@@ -93,12 +93,22 @@ struct HostBVH {
     ChildRec root4{};
     std::vector<Node4> nodes4;
     uint32_t stack4_bound = 0;  // most entries a 4-wide traversal can push
+    // instance definitions: one BVH each, shared by all their instances
+    std::vector<HostBVH> insts;
+    // With instances, the id a hit reports: refined primitives numbered in
+    // order with each instance taking as many ids as its definition has
+    // refined primitives (the ids of the same scene with every instance
+    // copied out).  flat_id[i] = first id of refined primitive i; empty
+    // without instances (id = refined index).
+    std::vector<uint32_t> flat_id;
+    uint64_t n_flat = 0;
 };
 
 // Fully refine shapes, build and flatten the BVH, and fill the device
 // layout.  Returns a PbrtStatus; *err gets a message on failure.
 int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_prims, const char* split_method,
-                   HostBVH* out, std::string* err, bool on_device = false);
+                   HostBVH* out, std::string* err, bool on_device = false, const PbrtInstanceDesc* defs = nullptr,
+                   uint32_t n_defs = 0);
 
 // Bounds (mesh.rs:196-205, sphere.rs:111-126) and centroids (bvh.rs:77) of
 // the refined primitives.

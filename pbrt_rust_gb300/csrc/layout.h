@@ -72,7 +72,10 @@ constexpr uint32_t kSphereBit = 0x80000000u;
 // (src/shape/disk.rs:16-22) or cylinder (src/shape/cylinder.rs:16-23) -
 // with its world-to-object and object-to-world matrix rows.  A disk keeps
 // its height in z_min = z_max (its object bound, disk.rs:70-74).
-enum { kQuadSphere = 0, kQuadDisk = 1, kQuadCylinder = 2 };
+// An instance (TransformedPrimitive) uses the same record: w2o / o2w are
+// its world-to-primitive / primitive-to-world matrices and `instance`
+// selects the definition's BVH.
+enum { kQuadSphere = 0, kQuadDisk = 1, kQuadCylinder = 2, kQuadInstance = 3 };
 struct alignas(16) SphereRec {
     float w2o[16];      // row-major world_to_object.m
     float o2w[16];      // row-major object_to_world.m
@@ -82,7 +85,7 @@ struct alignas(16) SphereRec {
     uint32_t flip;      // reverse_orientation ^ transform_swaps_handedness
     uint32_t kind;      // kQuad*
     float height, inner_radius;
-    uint32_t pad;
+    uint32_t instance;  // kQuadInstance: definition index
 };
 static_assert(sizeof(SphereRec) == 176, "analytic shape record is 176 bytes");
 

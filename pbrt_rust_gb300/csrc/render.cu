@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(128) k_shade(RenderParams P) {
 }
 
 // ---------------------------------------------------------------- shadow ---
-template <int STACK>
+template <int STACK, bool INST = false>
 __global__ void __launch_bounds__(128) k_shadow(RenderParams P) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= *(volatile uint32_t*)&P.counters[0]) return;
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(128) k_shadow(RenderParams P) {
     DRay r = make_dray(r4[2 * (size_t)q], r4[2 * (size_t)q + 1]);
     TraceResult res;
     int st = 0;
-    bool occ = traverse<STACK, true>(P.bvh, r, &res, &st);
+    bool occ = traverse<STACK, true, INST>(P.bvh, r, &res, &st);
     if (st) atomicMax((int*)&P.counters[2], st);
     P.occluded[P.shadow_slot[q]] = occ ? 1 : 0;
 }
@@ -101,8 +101,13 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
         uint64_t max_shadow = P.n_samples * P.n_lights;
         if (max_shadow) {
             const size_t smem = 16 * sizeof(uint2) * 128;
-            int wv = (P.has_wide && rk == 2) ? wide_stack_variant(P.wide_bound) : 0;
-            if (wv == 64)
+            const bool inst = P.bvh.insts != nullptr;
+            int wv = (P.has_wide && rk == 2 && !inst) ? wide_stack_variant(P.wide_bound) : 0;
+            if (inst && trace_stack_for_depth(P.depth) == 64)
+                k_shadow<64, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
+            else if (inst)
+                k_shadow<256, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
+            else if (wv == 64)
                 k_shadow4<16, 48><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
             else if (wv == 256)
                 k_shadow4<16, 240><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);

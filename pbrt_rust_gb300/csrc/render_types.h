@@ -29,6 +29,12 @@ struct alignas(16) ShadePrim {
 constexpr uint32_t kShadeFlip = 1u;
 constexpr uint32_t kShadeSphere = 2u;
 
+// Shading tables of one instance definition.
+struct InstShade {
+    const ShadePrim* shade;
+    const SphereRec* spheres;
+};
+
 enum { kLightPoint = 0, kLightArea = 1 };
 
 struct alignas(16) LightRec {
@@ -80,6 +86,12 @@ struct RenderParams {
     uint32_t n_lights;
     const AreaTri* area_tris;
     const float* area_cdf;
+    // instances (TransformedPrimitive): per instance primitive in id order
+    // (first hit id, refined index, definition size, analytic record), and
+    // per definition its shading tables; n_inst = 0 without instances
+    uint32_t n_inst;
+    const uint4* inst_map;
+    const InstShade* inst_defs;
     // buffers
     PbrtRay* rays;
     float4* hits;

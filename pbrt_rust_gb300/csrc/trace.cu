@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restr
 // different lengths then share warps without leaving lanes idle until the
 // longest one finishes.  Each ray's own traversal is unchanged, so results
 // are identical to k_trace.
-template <int STACK, bool ANY>
+template <int STACK, bool ANY, bool INST = false>
 __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
                                                           const uint32_t* __restrict__ order, float4* __restrict__ hits,
     uint8_t* __restrict__ occ,
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
     uint32_t ray = kNone;
     int st = 0;
     DRay r;
-    Traversal<STACK> T;
+    Traversal<STACK, INST> T;
     auto finish = [&]() {
         if (ANY)
             occ[ray] = T.found ? 1 : 0;
@@ -452,7 +452,7 @@ int wide_stack_variant(uint32_t bound) {
     return 0;
 }
 
-template <int STACK, bool ANY>
+template <int STACK, bool ANY, bool INST = false>
 static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                      float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream) {
     static int blocks_per_sm[2][2] = {{0, 0}, {0, 0}};
@@ -463,7 +463,7 @@ static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace_persistent<STACK, ANY>, block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace_persistent<STACK, ANY, INST>, block, 0);
         if (bps < 1) bps = 1;
     }
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
@@ -471,8 +471,8 @@ static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32
     if (per_warp < 32) per_warp = 32;
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace_persistent<STACK, ANY><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, occ, d_status, per_warp,
-                                                               g_refill);
+    k_trace_persistent<STACK, ANY, INST><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, occ, d_status, per_warp,
+                                                                     g_refill);
     return cudaGetLastError();
 }
 
@@ -487,6 +487,21 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
                          uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work) {
     if (n == 0) return cudaSuccess;
     read_variant();
+    if (bvh.insts) {
+        // a scene with instances: the binary-layout walk with nested
+        // instance traversal, whatever the configured kernel
+        const float4* r4 = reinterpret_cast<const float4*>(rays);
+        float4* h4 = reinterpret_cast<float4*>(hits);
+        const int stack = trace_stack_for_depth(depth);
+        const bool any = occluded != nullptr;
+        if (stack == 64)
+            return any ? launch_persistent<64, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
+                       : launch_persistent<64, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+        if (stack == 256)
+            return any ? launch_persistent<256, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
+                       : launch_persistent<256, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+        return cudaErrorInvalidValue;
+    }
     const int variant = kernel >= 0 ? kernel : g_kernel_variant;
     if (wide && variant == kVariantWideSpeculative) {
         const float4* r4 = reinterpret_cast<const float4*>(rays);

@@ -34,6 +34,7 @@ struct DevBVH {
     uint32_t has_spheres;
     uint32_t n_prims;
     uint32_t empty;
+    const DevBVH* insts;  // the instance definitions' BVHs (kQuadInstance records index it)
 };
 
 struct DRay {
@@ -263,12 +264,43 @@ struct TraceResult {
     float t, b1, b2;
 };
 
+// TransformedPrimitive::intersect / intersect_p (transformed.rs:35-59) for
+// the instance record `s`: the ray (o, d, tmin, maxt) is taken to primitive
+// space by w2p (the record's w2o) and traced through the definition's BVH.
+// Returns the definition-local hit (prim = its refined index, -1 on a miss);
+// the caller's maxt becomes the hit's t, as ray.set_maxt(r.maxt()) does.
+// Kept out of line so that the outer traversal's registers do not grow.
+template <bool ANY>
+__device__ __noinline__ TraceResult instance_test(const DevBVH* insts, const SphereRec* s, float ox, float oy,
+                                                  float oz, float dx, float dy, float dz, float tmin, float maxt);
+
+// One analytic primitive record: an instance (INST and kQuadInstance) or a
+// quadric (sphere_test).  *add gets the definition-local index of an
+// instance hit, 0 otherwise; *b1 / *b2 are left alone for quadrics.
+template <bool INST, bool ANY>
+__device__ __forceinline__ bool analytic_test(const SphereRec* spheres, const DevBVH* insts, uint32_t si,
+                                              const DRay& r, float maxt, float* t, float* b1, float* b2,
+                                              uint32_t* add) {
+    if (INST && spheres[si].kind == kQuadInstance) {
+        TraceResult q = instance_test<ANY>(insts, spheres + si, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.tmin, maxt);
+        if (q.prim < 0) return false;
+        *t = q.t;
+        *b1 = q.b1;
+        *b2 = q.b2;
+        *add = (uint32_t)q.prim;
+        return true;
+    }
+    return sphere_test(spheres, si, r, maxt, t);
+}
+
 // Per-ray traversal state.  start() tests the root box; step() does one
 // unit of work (one leaf's primitives, or one inner node's two child
 // boxes) and then, if needed, pops the next deferred child; it returns
 // false once the ray is finished.  Closest hit (ANY = false) or any hit
-// (ANY = true, stopping at the first accepted primitive).
-template <int STACK>
+// (ANY = true, stopping at the first accepted primitive).  INST: the
+// tree may hold instance records; kernels take INST only for scenes that
+// have instances, so the others keep the registers of the plain walk.
+template <int STACK, bool INST = false>
 struct Traversal {
     float maxt;
     uint32_t a, b;
@@ -307,10 +339,12 @@ struct Traversal {
                 float4 r0 = ldg4(pr->r0);
                 uint32_t id = __float_as_uint(r0.w);
                 float t, b1 = 0.0f, b2 = 0.0f;
+                uint32_t add = 0;
                 bool hit;
                 if (id & kSphereBit) {
                     float4 r1 = ldg4(pr->r1);
-                    hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
+                    hit = analytic_test<INST, ANY>(bvh.spheres, bvh.insts, __float_as_uint(r1.w), r, maxt, &t, &b1,
+                                                   &b2, &add);
                 } else {
                     float4 r1 = ldg4(pr->r1), r2 = ldg4(pr->r2);
                     hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
@@ -318,7 +352,7 @@ struct Traversal {
                 if (hit) {
                     maxt = t;
                     found = true;
-                    res.prim = (int32_t)(id & ~kSphereBit);
+                    res.prim = (int32_t)((id & ~kSphereBit) + add);
                     res.t = t;
                     res.b1 = b1;
                     res.b2 = b2;
@@ -375,15 +409,32 @@ struct Traversal {
 };
 
 // Whole traversal of one ray.
-template <int STACK, bool ANY>
+template <int STACK, bool ANY, bool INST = false>
 __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status) {
-    Traversal<STACK> T;
+    Traversal<STACK, INST> T;
     if (T.start(bvh, r)) {
         while (T.template step<ANY>(bvh, r, status)) {
         }
     }
     *res = T.res;
     return T.found;
+}
+
+// Definitions are at most kInstDepth levels deep (checked at creation), so
+// the nested stack never overflows.
+constexpr int kInstDepth = 64;
+
+template <bool ANY>
+__device__ __noinline__ TraceResult instance_test(const DevBVH* insts, const SphereRec* s, float ox, float oy,
+                                                  float oz, float dx, float dy, float dz, float tmin, float maxt) {
+    float o[3], d[3];
+    xf_point(s->w2o, ox, oy, oz, o);  // transform.rs:230-237: o as a point, d as a vector
+    xf_vector(s->w2o, dx, dy, dz, d);
+    const DRay ri = make_dray(make_float4(o[0], o[1], o[2], tmin), make_float4(d[0], d[1], d[2], maxt));
+    TraceResult res;
+    int status = 0;
+    traverse<kInstDepth, ANY, false>(insts[s->instance], ri, &res, &status);
+    return res;
 }
 
 }  // namespace pbrt

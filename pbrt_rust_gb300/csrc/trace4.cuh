@@ -19,6 +19,8 @@
 // [entry][thread] so a warp's accesses hit distinct banks) with an
 // optional local-memory overflow of OVF entries; the host picks a variant
 // whose SMAX + OVF covers the tree's bound (HostBVH::stack4_bound).
+// Trees holding instances are traced with the binary layout (Traversal
+// with INST), never with this one.
 #pragma once
 #include <stdint.h>
 

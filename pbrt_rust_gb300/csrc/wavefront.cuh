@@ -254,6 +254,79 @@ __device__ __forceinline__ void segment(V p1, float eps1, V p2, float eps2, Pbrt
     r->tmax = (1.0f - eps2) * dist;
 }
 
+// Hit point and geometric normal of refined primitive `sp` (its analytic
+// record in `spheres`) for the ray (ro, rd) at t: the dg.p / dg.nn that the
+// shape's intersect builds.
+__device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereRec* spheres, V ro, V rd, float t,
+                                              V* p_out, V* nn_out) {
+    const uint32_t flags = __float_as_uint(sp.c[3]);
+    V nn = mkv(0, 0, 1);
+    if ((flags & kShadeSphere) && spheres[flags >> 2].kind != kQuadSphere) {
+        const SphereRec& S = spheres[flags >> 2];
+        float o[3], d[3];
+        xf_point(S.w2o, ro.x, ro.y, ro.z, o);
+        xf_vector(S.w2o, rd.x, rd.y, rd.z, d);
+        const V ph = mkv(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
+        float pw[3];
+        xf_point(S.o2w, ph.x, ph.y, ph.z, pw);
+        *p_out = ld3(pw);
+        if (S.kind == kQuadDisk) {
+            // disk.rs:106-129: the normal is the transformed +-z (by the
+            // side of the object-space ray origin), neither normalised
+            // nor flipped
+            const float nz = o[2] > 0.0f ? 1.0f : -1.0f;  // transform.rs:220-227 (inverse transpose)
+            nn = mkv(S.w2o[0] * 0.0f + S.w2o[4] * 0.0f + S.w2o[8] * nz,
+                     S.w2o[1] * 0.0f + S.w2o[5] * 0.0f + S.w2o[9] * nz,
+                     S.w2o[2] * 0.0f + S.w2o[6] * 0.0f + S.w2o[10] * nz);
+        } else {
+            // cylinder.rs:143-164 + helpers.rs:17-43 + diff_geom.rs:52-79
+            V dpdu = mkv(S.phi_max * -ph.y, S.phi_max * ph.x, 0.0f);
+            V dpdv = mkv(0.0f, 0.0f, S.z_max - S.z_min);
+            float du[3], dv[3];
+            xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
+            xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
+            nn = vnorm(vcross(ld3(du), ld3(dv)));
+            if (S.flip) nn = vmul(nn, -1.0f);
+        }
+    } else if (flags & kShadeSphere) {
+        // sphere.rs:135-176 + shape/helpers.rs:17-43 + diff_geom.rs:52-79
+        const SphereRec& S = spheres[flags >> 2];
+        float o[3], d[3];
+        xf_point(S.w2o, ro.x, ro.y, ro.z, o);
+        xf_vector(S.w2o, rd.x, rd.y, rd.z, d);
+        V ph = mkv(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
+        float zc = ph.z / S.radius;
+        zc = zc < -1.0f ? -1.0f : (zc > 1.0f ? 1.0f : zc);
+        float theta = acosf(zc);
+        float zradius = sqrtf(ph.x * ph.x + ph.y * ph.y);
+        float inv_zr = 1.0f / zradius;
+        float cos_phi = ph.x * inv_zr, sin_phi = ph.y * inv_zr;
+        float dtheta = S.theta_max - S.theta_min;
+        V dpdu = mkv(-S.phi_max * ph.y, S.phi_max * ph.x, 0.0f);
+        V dpdv = vmul(mkv(ph.z * cos_phi, ph.z * sin_phi, -S.radius * sinf(theta)), dtheta);
+        float pw[3], du[3], dv[3];
+        xf_point(S.o2w, ph.x, ph.y, ph.z, pw);
+        xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
+        xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
+        *p_out = ld3(pw);
+        nn = vnorm(vcross(ld3(du), ld3(dv)));
+        if (S.flip) nn = vmul(nn, -1.0f);
+    } else {
+        // mesh.rs:212-264 with the default uvs: du1 = -1, du2 = 0,
+        // dv1 = -1, dv2 = -1, determinant 1
+        V p1 = ld3(sp.a), p2 = ld3(sp.b), p3 = ld3(sp.c);
+        const float du1 = 0.0f - 1.0f, du2 = 1.0f - 1.0f, dv1 = 0.0f - 1.0f, dv2 = 0.0f - 1.0f;
+        V dp1 = vsub(p1, p3), dp2 = vsub(p2, p3);
+        float inv_det = 1.0f / (du1 * dv2 - dv1 * du2);
+        V dpdu = vmul(vsub(vmul(dp1, dv2), vmul(dp2, dv1)), inv_det);
+        V dpdv = vmul(vadd(vmul(dp1, -du2), vmul(dp2, du1)), inv_det);
+        *p_out = mkv(ro.x + rd.x * t, ro.y + rd.y * t, ro.z + rd.z * t);
+        nn = vnorm(vcross(dpdu, dpdv));
+        if (flags & kShadeFlip) nn = vmul(nn, -1.0f);
+    }
+    *nn_out = nn;
+}
+
 // Where shade_sample appends its shadow rays: the ray, the (sample, light)
 // slot it decides and, in a batch, the job it belongs to.
 struct ShadowSink {
@@ -283,70 +356,52 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
     if (hit) {
         const PbrtRay r = P.rays[s];
         float t = h.y;
-        const ShadePrim& sp = P.shade[prim];
-        uint32_t flags = __float_as_uint(sp.c[3]);
-        if ((flags & kShadeSphere) && P.spheres[flags >> 2].kind != kQuadSphere) {
-            const SphereRec& S = P.spheres[flags >> 2];
-            float o[3], d[3];
-            xf_point(S.w2o, r.ox, r.oy, r.oz, o);
-            xf_vector(S.w2o, r.dx, r.dy, r.dz, d);
-            const V ph = mkv(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
-            float pw[3];
-            xf_point(S.o2w, ph.x, ph.y, ph.z, pw);
-            p = ld3(pw);
-            if (S.kind == kQuadDisk) {
-                // disk.rs:106-129: the normal is the transformed +-z (by the
-                // side of the object-space ray origin), neither normalised
-                // nor flipped
-                const float nz = o[2] > 0.0f ? 1.0f : -1.0f;  // transform.rs:220-227 (inverse transpose)
-                nn = mkv(S.w2o[0] * 0.0f + S.w2o[4] * 0.0f + S.w2o[8] * nz,
-                         S.w2o[1] * 0.0f + S.w2o[5] * 0.0f + S.w2o[9] * nz,
-                         S.w2o[2] * 0.0f + S.w2o[6] * 0.0f + S.w2o[10] * nz);
-            } else {
-                // cylinder.rs:143-164 + helpers.rs:17-43 + diff_geom.rs:52-79
-                V dpdu = mkv(S.phi_max * -ph.y, S.phi_max * ph.x, 0.0f);
-                V dpdv = mkv(0.0f, 0.0f, S.z_max - S.z_min);
-                float du[3], dv[3];
-                xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
-                xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
-                nn = vnorm(vcross(ld3(du), ld3(dv)));
-                if (S.flip) nn = vmul(nn, -1.0f);
+        V o = mkv(r.ox, r.oy, r.oz), d = mkv(r.dx, r.dy, r.dz);
+        const ShadePrim* shade = P.shade;
+        const SphereRec* spheres = P.spheres;
+        const SphereRec* inst = nullptr;
+        uint32_t id = (uint32_t)prim;
+        if (P.n_inst) {
+            // the last instance whose first id is <= id (ids are in refined order)
+            uint32_t lo = 0, hi = P.n_inst;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (P.inst_map[mid].x <= id)
+                    lo = mid + 1;
+                else
+                    hi = mid;
             }
-        } else if (flags & kShadeSphere) {
-            // sphere.rs:135-176 + shape/helpers.rs:17-43 + diff_geom.rs:52-79
-            const SphereRec& S = P.spheres[flags >> 2];
-            float o[3], d[3];
-            xf_point(S.w2o, r.ox, r.oy, r.oz, o);
-            xf_vector(S.w2o, r.dx, r.dy, r.dz, d);
-            V ph = mkv(o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t);
-            float zc = ph.z / S.radius;
-            zc = zc < -1.0f ? -1.0f : (zc > 1.0f ? 1.0f : zc);
-            float theta = acosf(zc);
-            float zradius = sqrtf(ph.x * ph.x + ph.y * ph.y);
-            float inv_zr = 1.0f / zradius;
-            float cos_phi = ph.x * inv_zr, sin_phi = ph.y * inv_zr;
-            float dtheta = S.theta_max - S.theta_min;
-            V dpdu = mkv(-S.phi_max * ph.y, S.phi_max * ph.x, 0.0f);
-            V dpdv = vmul(mkv(ph.z * cos_phi, ph.z * sin_phi, -S.radius * sinf(theta)), dtheta);
-            float pw[3], du[3], dv[3];
-            xf_point(S.o2w, ph.x, ph.y, ph.z, pw);
-            xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
-            xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
+            if (lo > 0) {
+                const uint4 e = P.inst_map[lo - 1];
+                if (id - e.x < e.z) {
+                    // inside the instance: shade the definition's primitive on
+                    // the primitive-space ray (transformed.rs:37-38)
+                    inst = P.spheres + e.w;
+                    const InstShade D = P.inst_defs[inst->instance];
+                    shade = D.shade;
+                    spheres = D.spheres;
+                    id -= e.x;
+                    float oi[3], di[3];
+                    xf_point(inst->w2o, o.x, o.y, o.z, oi);
+                    xf_vector(inst->w2o, d.x, d.y, d.z, di);
+                    o = ld3(oi);
+                    d = ld3(di);
+                } else {
+                    id = e.y + 1u + (id - e.x - e.z);  // a primitive after that instance
+                }
+            }
+        }
+        const ShadePrim& sp = shade[id];
+        surface_point(sp, spheres, o, d, t, &p, &nn);
+        if (inst) {
+            // transformed.rs:45-47: p by primitive-to-world, nn by its
+            // normal transform (w2p transposed), normalised
+            float pw[3];
+            xf_point(inst->o2w, p.x, p.y, p.z, pw);
             p = ld3(pw);
-            nn = vnorm(vcross(ld3(du), ld3(dv)));
-            if (S.flip) nn = vmul(nn, -1.0f);
-        } else {
-            // mesh.rs:212-264 with the default uvs: du1 = -1, du2 = 0,
-            // dv1 = -1, dv2 = -1, determinant 1
-            V p1 = ld3(sp.a), p2 = ld3(sp.b), p3 = ld3(sp.c);
-            const float du1 = 0.0f - 1.0f, du2 = 1.0f - 1.0f, dv1 = 0.0f - 1.0f, dv2 = 0.0f - 1.0f;
-            V dp1 = vsub(p1, p3), dp2 = vsub(p2, p3);
-            float inv_det = 1.0f / (du1 * dv2 - dv1 * du2);
-            V dpdu = vmul(vsub(vmul(dp1, dv2), vmul(dp2, dv1)), inv_det);
-            V dpdv = vmul(vadd(vmul(dp1, -du2), vmul(dp2, du1)), inv_det);
-            p = mkv(r.ox + r.dx * t, r.oy + r.dy * t, r.oz + r.dz * t);
-            nn = vnorm(vcross(dpdu, dpdv));
-            if (flags & kShadeFlip) nn = vmul(nn, -1.0f);
+            const float* m = inst->w2o;
+            nn = vnorm(mkv(m[0] * nn.x + m[4] * nn.y + m[8] * nn.z, m[1] * nn.x + m[5] * nn.y + m[9] * nn.z,
+                           m[2] * nn.x + m[6] * nn.y + m[10] * nn.z));
         }
         eps = t * 5e-4f;  // mesh.rs:262, sphere.rs:174
         wo = mkv(-r.dx, -r.dy, -r.dz);

@@ -12,16 +12,21 @@ float32.
                 quad area light, 2x2 jittered strata
   heightfield   708x708-vertex terrain (999,698 triangles) + area light,
                 1024x1024 at 16 spp, and 2^22 incoherent rays
+  instanced_forest  two object definitions (a triangle "tree" with a sphere
+                crown and a disk base; a cylinder with a mesh cap) placed by
+                rotated, scaled TransformedPrimitive instances on a ground
+                quad, point + area light
 """
 from __future__ import annotations
 
+import dataclasses
 import math
 
 import numpy as np
 
 from . import abi
-from .scene import (Camera, DiffuseAreaLight, Film, Filter, MatteMaterial, PointLight, Primitive, Shape,
-                    StratifiedSampler)
+from .scene import (Camera, DiffuseAreaLight, Film, Filter, InstanceDefinition, MatteMaterial, PointLight,
+                    Primitive, Shape, StratifiedSampler)
 from .transform import Transform
 
 _MUL = 6364136223846793005
@@ -317,3 +322,68 @@ def poisson_arrivals(n: int, rate: float, seed: int = 0) -> np.ndarray:
     second: cumulative sums of exponential gaps drawn by inversion."""
     u = PCG32(seed).uniform(n)
     return np.cumsum(-np.log1p(-u) / rate)
+
+
+def instanced_forest(n_instances: int = 64, tris_per_tree: int = 2000, seed: int | None = None, res: int = 128,
+                     spp_side: int = 2):
+    """Two definitions in instance space: a "tree" (a triangle soup cone of
+    `tris_per_tree` triangles in y [0, 2], a sphere crown of radius 0.6 at
+    y = 2.2, a disk base of radius 0.5 rotated to face +y) and a "post" (a
+    cylinder of radius 0.15 along y with a 2-triangle cap).  Instance k:
+    rotate(360 u0, y) and uniform scale 0.5 + u1, translated to
+    (-8 + 16 u2, 0, -8 + 16 u3); even k use the tree.  Ground quad
+    (y = 0, [-10, 10]^2), point light, quad area light at y = 6.  Returns
+    (prims, lights, camera, sampler, flat) where `flat` has every instance
+    copied out shape by shape with the composed transform (the same scene
+    without instancing)."""
+    rng = PCG32(config_seed(7) if seed is None else seed)
+    n = tris_per_tree
+    u = rng.uniform(12 * n).reshape(n, 12)
+    h = 2.0 * u[:, 0]
+    ang = 2.0 * math.pi * u[:, 1]
+    rad = 0.6 * (1.0 - h / 2.0) * np.sqrt(u[:, 2])
+    cen = np.stack([rad * np.cos(ang), h, rad * np.sin(ang)], axis=-1)
+    off = (u[:, 3:12].reshape(n, 3, 3) * 2.0 - 1.0) * 0.08
+    pts = (cen[:, None, :] + off).reshape(-1, 3).astype(np.float32)
+    bark, leaf, stone = MatteMaterial((0.45, 0.3, 0.15)), MatteMaterial((0.2, 0.6, 0.25)), MatteMaterial((0.6,) * 3)
+    tree = InstanceDefinition([
+        Primitive.geometric(Shape.triangle_mesh(Transform(), None, False, np.arange(3 * n, dtype=np.uint32), pts),
+                            leaf),
+        Primitive.geometric(Shape.sphere(Transform.translate((0.0, 2.2, 0.0)), None, False, 0.6, -0.6, 0.6, 360.0),
+                            leaf),
+        Primitive.geometric(Shape.disk(Transform.rotate(-90.0, (1.0, 0.0, 0.0)), None, False, 0.01, 0.5, 0.0,
+                                       360.0), bark),
+    ])
+    cap = np.array([(-0.2, 1.5, -0.2), (0.2, 1.5, -0.2), (0.2, 1.5, 0.2), (-0.2, 1.5, 0.2)], np.float32)
+    post = InstanceDefinition([
+        Primitive.geometric(Shape.cylinder(Transform.rotate(-90.0, (1.0, 0.0, 0.0)), None, False, 0.15, 0.0, 1.5,
+                                           360.0), stone),
+        Primitive.geometric(Shape.triangle_mesh(Transform(), None, False, np.array([0, 2, 1, 0, 3, 2], np.uint32),
+                                                cap), stone),
+    ])
+    ground_pts = np.array([(-10, 0, -10), (10, 0, -10), (10, 0, 10), (-10, 0, 10)], np.float32)
+    ground = Primitive.geometric(
+        Shape.triangle_mesh(Transform(), None, False, np.array([0, 1, 2, 0, 2, 3], np.uint32), ground_pts),
+        MatteMaterial((0.5, 0.5, 0.5)))
+    prims, flat = [ground], [ground]
+    v = rng.uniform(4 * n_instances).reshape(n_instances, 4)
+    for k in range(n_instances):
+        sc = 0.5 + float(v[k, 1])
+        i2w = (Transform.translate((-8.0 + 16.0 * float(v[k, 2]), 0.0, -8.0 + 16.0 * float(v[k, 3])))
+               * Transform.rotate(360.0 * float(v[k, 0]), (0.0, 1.0, 0.0)) * Transform.scale(sc, sc, sc))
+        defn = tree if k % 2 == 0 else post
+        prims.append(Primitive.transformed(defn, i2w.inverse()))
+        for q in defn.prims:
+            flat.append(Primitive.geometric(dataclasses.replace(q.shape, object_to_world=i2w * q.shape.object_to_world),
+                                            q.material))
+    lights = [PointLight(Transform.translate((3.0, 7.0, -4.0)), (120.0, 120.0, 120.0))]
+    area = DiffuseAreaLight(Transform(), (8.0, 8.0, 8.0))
+    lamp = Primitive.geometric_area_light(quad_light_mesh((0.0, 6.0, 0.0), 2.0), MatteMaterial((0, 0, 0)), area)
+    prims.append(lamp)
+    flat.append(lamp)
+    lights.append(area)
+    cam2world = Transform.look_at((0.0, 6.0, -14.0), (0.0, 0.5, 0.0), (0.0, 1.0, 0.0)).inverse()
+    film = Film.image(res, res, Filter.mean(0.5, 0.5))
+    camera = Camera.perspective(cam2world, (-1.0, 1.0, -1.0, 1.0), 0.0, 1.0, 0.0, 1e30, 55.0, film)
+    sampler = StratifiedSampler.stratified(0, res, 0, res, spp_side, spp_side, True, 0.0, 1.0)
+    return prims, lights, camera, sampler, flat

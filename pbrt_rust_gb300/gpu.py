@@ -79,10 +79,14 @@ class GpuBVHAccel:
         prims = [p if isinstance(p, Primitive) else Primitive.simple(p) for p in prims]
         self.desc = SceneDescription(prims, [], max_prims, split_method, aggregate_only=True)
         h = C.c_void_p()
-        abi.check(self._lib.pbrtgpu_bvh_create_ex(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
-                                                  split_method.encode(),
-                                                  abi.BUILD_ON_DEVICE if build_on_device else 0, C.byref(h)),
-                  self._lib)
+        flags = abi.BUILD_ON_DEVICE if build_on_device else 0
+        if self.desc.definitions:  # TransformedPrimitive instances among the primitives
+            self.desc.desc.build_flags = flags
+            abi.check(self._lib.pbrtgpu_bvh_create_desc(C.byref(self.desc.desc), C.byref(h)), self._lib)
+        else:
+            abi.check(self._lib.pbrtgpu_bvh_create_ex(self.desc.shapes, self.desc.desc.n_shapes, int(max_prims),
+                                                      split_method.encode(), flags, C.byref(h)),
+                      self._lib)
         self._h = h
         self._own = True
 

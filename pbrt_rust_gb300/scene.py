@@ -36,6 +36,7 @@ class Shape:
     phi_max: float = 360.0
     height: float = 0.0        # disk
     inner_radius: float = 0.0  # disk
+    definition: "InstanceDefinition | None" = None  # instance: the shared primitives
 
     @staticmethod
     def triangle_mesh(o2w: Transform, w2o: Transform | None, ro: bool, vi, p) -> "Shape":
@@ -74,6 +75,25 @@ class Shape:
 
     def num_primitives(self) -> int:
         return len(self.indices) // 3 if self.kind == abi.SHAPE_TRIANGLE_MESH else 1
+
+    def num_ids(self) -> int:
+        """Hit ids the shape takes: an instance takes one per refined
+        primitive of its definition."""
+        if self.kind == abi.SHAPE_INSTANCE:
+            return self.definition.num_primitives()
+        return self.num_primitives()
+
+
+@dataclass(eq=False)
+class InstanceDefinition:
+    """The primitives of one ObjectBegin ... ObjectEnd block
+    (src/main.rs:714-733) in instance space, shared by all its instances:
+    one BVH over them is built once per scene.  They hold no area lights
+    and no instances."""
+    prims: list
+
+    def num_primitives(self) -> int:
+        return sum(p.shape.num_primitives() for p in self.prims)
 
 
 @dataclass
@@ -114,6 +134,23 @@ class Primitive:
         return Primitive(s, MatteMaterial())
 
     @staticmethod
+    def transformed(defn: InstanceDefinition, world_to_primitive: Transform) -> "Primitive":
+        """Primitive::transformed (src/primitive/mod.rs:101-106) with a
+        static transform: TransformedPrimitive (transformed.rs:14-59) over
+        the definition's aggregate.  Hits inside it report the id
+        (first id of the instance) + (refined index inside the
+        definition)."""
+        if not isinstance(defn, InstanceDefinition):
+            raise TypeError("an instance refers to an InstanceDefinition")
+        if not defn.prims:
+            raise ValueError("instance of an empty definition")
+        for p in defn.prims:
+            if p.area_light is not None or p.shape.kind == abi.SHAPE_INSTANCE:
+                raise ValueError("instance definitions hold neither area lights nor instances")
+        shape = Shape(abi.SHAPE_INSTANCE, world_to_primitive.inverse(), definition=defn)
+        return Primitive(shape, MatteMaterial())
+
+    @staticmethod
     def geometric_area_light(s: Shape, mtl: MatteMaterial, al: DiffuseAreaLight) -> "Primitive":
         if s.kind != abi.SHAPE_TRIANGLE_MESH:
             raise ValueError("area lights are supported on triangle meshes")
@@ -132,35 +169,28 @@ class SceneDescription:
         self._keep = []
         mats: list[MatteMaterial] = []
         mat_index: dict[int, int] = {}
+        defs: list[InstanceDefinition] = []
+        def_index: dict[int, int] = {}
         for p in self.prims:
-            if id(p.material) not in mat_index:
+            d = p.shape.definition if p.shape.kind == abi.SHAPE_INSTANCE else None
+            if d is not None and id(d) not in def_index:
+                def_index[id(d)] = len(defs)
+                defs.append(d)
+        for p in self.prims + [q for d in defs for q in d.prims]:
+            if p.shape.kind != abi.SHAPE_INSTANCE and id(p.material) not in mat_index:
                 mat_index[id(p.material)] = len(mats)
                 mats.append(p.material)
         light_index = {id(l): i for i, l in enumerate(self.lights)}
         shape_index = {id(p.shape): i for i, p in enumerate(self.prims)}
         n = len(self.prims)
-        self.shapes = (abi.PbrtShapeDesc * max(n, 1))()
-        for i, p in enumerate(self.prims):
-            s = p.shape
-            d = self.shapes[i]
-            d.kind = s.kind
-            d.reverse_orientation = int(s.reverse_orientation)
-            d.object_to_world = s.object_to_world.to_abi()
-            if s.kind == abi.SHAPE_TRIANGLE_MESH:
-                self._keep += [s.points, s.indices]
-                d.points = abi.f32p(s.points)
-                d.n_points = len(s.points)
-                d.indices = abi.u32p(s.indices)
-                d.n_indices = len(s.indices)
-            d.radius, d.z0, d.z1, d.phi_max_deg = s.radius, s.z0, s.z1, s.phi_max
-            d.height, d.inner_radius = s.height, s.inner_radius
-            d.material = mat_index[id(p.material)]
-            if p.area_light is not None and not aggregate_only:
-                if id(p.area_light) not in light_index:
-                    raise ValueError("an area light of a primitive is missing from the scene's lights")
-                d.area_light = light_index[id(p.area_light)]
-            else:
-                d.area_light = -1
+        self.shapes = self._shape_array(self.prims, mat_index, def_index, light_index, aggregate_only)
+        # instance definitions, their shapes marshalled like the scene's
+        self.definitions = defs
+        self.def_shapes = [self._shape_array(d.prims, mat_index, {}, {}, True) for d in defs]
+        self.instance_descs = (abi.PbrtInstanceDesc * max(len(defs), 1))()
+        for k, d in enumerate(defs):
+            self.instance_descs[k].shapes = self.def_shapes[k]
+            self.instance_descs[k].n_shapes = len(d.prims)
         self.materials = (abi.PbrtMaterialDesc * max(len(mats), 1))()
         for i, m in enumerate(mats):
             self.materials[i].kd[:] = [float(c) for c in m.kd]
@@ -193,9 +223,48 @@ class SceneDescription:
         self.desc.n_lights = len(self.lights)
         self.desc.max_prims_in_node = int(max_prims)
         self.desc.split_method = abi.SPLIT_METHODS.get(split_method, 0)
+        self.desc.instances = self.instance_descs
+        self.desc.n_instances = len(defs)
+
+    def _shape_array(self, prims, mat_index, def_index, light_index, aggregate_only):
+        arr = (abi.PbrtShapeDesc * max(len(prims), 1))()
+        for i, p in enumerate(prims):
+            s = p.shape
+            d = arr[i]
+            d.kind = s.kind
+            d.reverse_orientation = int(s.reverse_orientation)
+            d.object_to_world = s.object_to_world.to_abi()
+            if s.kind == abi.SHAPE_TRIANGLE_MESH:
+                self._keep += [s.points, s.indices]
+                d.points = abi.f32p(s.points)
+                d.n_points = len(s.points)
+                d.indices = abi.u32p(s.indices)
+                d.n_indices = len(s.indices)
+            d.radius, d.z0, d.z1, d.phi_max_deg = s.radius, s.z0, s.z1, s.phi_max
+            d.height, d.inner_radius = s.height, s.inner_radius
+            if s.kind == abi.SHAPE_INSTANCE:
+                if id(s.definition) not in def_index:
+                    raise ValueError("instance definitions hold no instances")
+                d.instance = def_index[id(s.definition)]
+                d.material = 0
+            else:
+                d.instance = -1
+                d.material = mat_index[id(p.material)]
+            if p.area_light is not None and not aggregate_only:
+                if id(p.area_light) not in light_index:
+                    raise ValueError("an area light of a primitive is missing from the scene's lights")
+                d.area_light = light_index[id(p.area_light)]
+            else:
+                d.area_light = -1
+        return arr
 
     def num_primitives(self) -> int:
         return sum(p.shape.num_primitives() for p in self.prims)
+
+    def num_ids(self) -> int:
+        """Ids hits report: refined primitives with every instance counted
+        out (equal to num_primitives without instances)."""
+        return sum(p.shape.num_ids() for p in self.prims)
 
 
 # ---------------------------------------------------------- camera & film --

@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_status_strings(lib):
-    assert lib.pbrtgpu_abi_version() == 1
+    assert lib.pbrtgpu_abi_version() == abi.ABI_VERSION == 2
     assert lib.pbrtgpu_status_str(0) == b"ok"
     assert lib.pbrtgpu_status_str(6) == b"traversal stack overflow"
     assert lib.pbrtgpu_status_str(999) == b"unknown status"
