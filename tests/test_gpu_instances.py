@@ -7,7 +7,7 @@ within the render tests' 1e-4 (sphere normals go through acosf/sinf)."""
 import numpy as np
 import pytest
 
-from pbrt_rust_gb300 import generators as G
+from pbrt_rust_gb300 import abi, generators as G
 from pbrt_rust_gb300.batch import GpuBatch
 from pbrt_rust_gb300.gpu import GpuBVHAccel, GpuSamplerRenderer, GpuScene
 from pbrt_rust_gb300.scene import SceneDescription, default_num_tasks
@@ -31,11 +31,14 @@ def test_instance_ids_cover_every_definition_primitive(oracle):
     """Hits land inside many instances and on primitives of both
     definitions; ids stay below the counted-out total."""
     prims, _, _, _, _ = G.instanced_forest(n_instances=16, tris_per_tree=200, seed=2)
-    total = SceneDescription(prims, []).num_ids()
+    total = SceneDescription(prims, [], aggregate_only=True).num_ids()
     rays = G.rays_toward_center(G.PCG32(9), 1 << 15, radius=14.0, target=4.0)
     h = GpuBVHAccel(prims).intersect(rays)
     ids = h["prim"][h["prim"] >= 0]
-    assert ids.max() < total and len(np.unique(ids)) > 500
+    assert ids.max() < total and len(np.unique(ids)) > 100
+    first = np.cumsum([0] + [p.shape.num_ids() for p in prims])[:-1]
+    owner = np.searchsorted(first, ids, side="right") - 1
+    assert sum(prims[k].shape.kind == abi.SHAPE_INSTANCE for k in set(owner.tolist())) == 16
 
 
 def test_instanced_render_matches_oracle(oracle):
