@@ -319,6 +319,51 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 400, 
             "poisson_mean_batch": poisson["mean_batch_requests"], "bit_exact": exact}
 
 
+def bench_instanced(torch, dev, stream, n_instances: int = 256, tris_per_tree: int = 20000,
+                    n_rays: int = 1 << 22):
+    """TransformedPrimitive instancing: the instanced forest against the
+    same forest with every instance copied out, closest hit of 2^22 rays
+    aimed into the forest (device-resident rays, CUDA events, L2 flushed)."""
+    from pbrt_rust_gb300 import abi, generators as G
+    from pbrt_rust_gb300.gpu import GpuBVHAccel
+    lib = abi.load()
+    prims, _, _, _, flat = G.instanced_forest(n_instances=n_instances, tris_per_tree=tris_per_tree, seed=1)
+    rays = G.rays_toward_center(G.PCG32(77), n_rays, radius=14.0, target=4.0)
+    inst = GpuBVHAccel(prims, 4, "sah", build_on_device=True)
+    copied = GpuBVHAccel(flat, 4, "sah", build_on_device=True)
+    sh = C.c_void_p(stream.cuda_stream)
+    rays_dev = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    out = {}
+    hits = {}
+    for name, b in (("instanced", inst), ("copied_out", copied)):
+        h = torch.empty((n_rays, 4), dtype=torch.float32, device=dev)
+        rp, hp = C.c_void_p(rays_dev.data_ptr()), C.c_void_p(h.data_ptr())
+        ms = []
+        with torch.cuda.stream(stream):
+            for k in range(8):
+                flush.zero_()
+                a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                abi.check(lib.pbrtgpu_intersect(b._h, rp, n_rays, hp, sh), lib)
+                e.record(stream)
+                if k >= 3:
+                    ms.append((a, e))
+        torch.cuda.synchronize(dev)
+        t = statistics.mean(a.elapsed_time(e) for a, e in ms)
+        out[name] = {"mrays_s": n_rays / t / 1e3, "ms": t, "device_bytes": b.device_bytes(),
+                     "primitives": b.num_primitives(), "nodes": b.num_nodes()}
+        hits[name] = h
+    agree = (hits["instanced"][:, 0].view(torch.int32) == hits["copied_out"][:, 0].view(torch.int32))
+    out.update({"instances": n_instances, "tris_per_tree": tris_per_tree,
+                "copied_out_triangles": sum(p.shape.num_primitives() for p in flat),
+                "same_hit_fraction": float(agree.float().mean().item()),
+                "memory_ratio": out["copied_out"]["device_bytes"] / out["instanced"]["device_bytes"],
+                "what": "forest of tree/post definitions placed by rotated, scaled instances; closest hit of "
+                        "2^22 rays aimed into it; hit ids of the two scenes agree up to f32 rounding"})
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -456,6 +501,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         renderer.render(scene, out=img, stream=stream)
         rt.append(time.perf_counter() - t0)
+    instanced = bench_instanced(torch, dev, stream)
     batched = bench_batched(torch, dev, stream) if not args.skip_multi else None
     served = bench_served(torch, dev, stream) if not args.skip_multi else None
     clk.__exit__(None, None, None)
@@ -499,6 +545,7 @@ def run_ours(args):
                                        "camera_rays": 1024 * 1024 * 16},
             "bvh_build": {"host_s": build_s, "device_s": dbuild_s, "identical": same_tree,
                           "what": "pbrtgpu_bvh_create(_ex) of the 1M-triangle heightfield, host vs device tree build"},
+            "instancing": instanced,
             "batched_multi_scene": batched,
             "served": served,
         }

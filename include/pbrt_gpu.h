@@ -244,6 +244,10 @@ void pbrtgpu_bvh_destroy(PbrtBVH* bvh);
 /* Replaces HasBounds::world_bound for BVHAccelerator (bvh.rs:365-373). */
 int pbrtgpu_bvh_world_bound(const PbrtBVH* bvh, float lo[3], float hi[3]);
 int pbrtgpu_bvh_num_primitives(const PbrtBVH* bvh, uint32_t* n);
+/* Device memory the aggregate keeps resident (node layouts, primitive and
+ * analytic records, instance definitions); no counterpart in the
+ * reference. */
+int pbrtgpu_bvh_device_bytes(const PbrtBVH* bvh, uint64_t* bytes);
 int pbrtgpu_bvh_num_nodes(const PbrtBVH* bvh, uint32_t* n);
 int pbrtgpu_bvh_depth(const PbrtBVH* bvh, uint32_t* depth);
 /* The reference-order linearised nodes (bvh.rs:319-325). */

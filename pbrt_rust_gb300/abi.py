@@ -171,6 +171,7 @@ SIGNATURES = {
     "pbrtgpu_bvh_destroy": (None, [_P]),
     "pbrtgpu_bvh_world_bound": (C.c_int, [_P, _F3, _F3]),
     "pbrtgpu_bvh_num_primitives": (C.c_int, [_P, _U32P]),
+    "pbrtgpu_bvh_device_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "pbrtgpu_bvh_num_nodes": (C.c_int, [_P, _U32P]),
     "pbrtgpu_bvh_depth": (C.c_int, [_P, _U32P]),
     "pbrtgpu_bvh_get_nodes": (C.c_int, [_P, _P, C.c_uint32]),

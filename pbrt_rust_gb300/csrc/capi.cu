@@ -100,26 +100,24 @@ int bvh_upload(PbrtBVH* b) {
     if ((st = upload(&b->d_nodes4, b->host.nodes4))) return st;
     if ((st = cuda_status(cudaMalloc(&b->d_status, sizeof(int)), "cudaMalloc"))) return st;
     if ((st = cuda_status(cudaMemset(b->d_status, 0, sizeof(int)), "cudaMemset"))) return st;
-    // instance definitions: binary layout, traced by instance_test
-    std::vector<DevBVH> defs;
+    // instance definitions: 4-wide layout, walked by instance_test
+    std::vector<DevBVH4> defs;
     for (const HostBVH& I : b->host.insts) {
-        NodePair* pairs = nullptr;
+        Node4* nodes = nullptr;
         PrimRec* prims = nullptr;
         SphereRec* spheres = nullptr;
-        st = upload(&pairs, I.pairs);
-        if (pairs) b->d_inst_bufs.push_back(pairs);
+        st = upload(&nodes, I.nodes4);
+        if (nodes) b->d_inst_bufs.push_back(nodes);
         if (!st) st = upload(&prims, I.recs);
         if (prims) b->d_inst_bufs.push_back(prims);
         if (!st) st = upload(&spheres, I.spheres);
         if (spheres) b->d_inst_bufs.push_back(spheres);
         if (st) return st;
-        DevBVH d{};
-        d.pairs = pairs;
+        DevBVH4 d{};
+        d.nodes = nodes;
         d.prims = prims;
         d.spheres = spheres;
-        d.root = I.root;
-        d.has_spheres = I.has_spheres ? 1u : 0u;
-        d.n_prims = (uint32_t)I.recs.size();
+        d.root = I.root4;
         d.empty = I.nodes.empty() ? 1u : 0u;
         d.insts = nullptr;
         defs.push_back(d);
@@ -127,6 +125,7 @@ int bvh_upload(PbrtBVH* b) {
     b->inst_dev = defs;
     if ((st = upload(&b->d_insts, defs))) return st;
     b->dev.insts = b->d_insts;
+    b->dev4.insts = b->d_insts;
     b->dev.pairs = b->d_pairs;
     b->dev.prims = b->d_prims;
     b->dev.spheres = b->d_spheres;
@@ -143,10 +142,8 @@ int bvh_upload(PbrtBVH* b) {
     return PBRT_OK;
 }
 
-// The 4-wide layout when a compiled variant covers its stack bound (never
-// for a tree with instances: those take the binary walk).
+// The 4-wide layout when a compiled variant covers its stack bound.
 const DevBVH4* wide_of(const PbrtBVH* b) {
-    if (!b->host.insts.empty()) return nullptr;
     return wide_stack_variant(b->host.stack4_bound) ? &b->dev4 : nullptr;
 }
 
@@ -384,6 +381,17 @@ int pbrtgpu_bvh_world_bound(const PbrtBVH* b, float lo[3], float hi[3]) {
 int pbrtgpu_bvh_num_primitives(const PbrtBVH* b, uint32_t* n) {
     if (!b || !n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     *n = (uint32_t)b->host.prims.size();
+    return PBRT_OK;
+}
+int pbrtgpu_bvh_device_bytes(const PbrtBVH* b, uint64_t* bytes) {
+    if (!b || !bytes) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    const HostBVH& H = b->host;
+    uint64_t n = H.pairs.size() * sizeof(NodePair) + H.recs.size() * sizeof(PrimRec) +
+                 H.spheres.size() * sizeof(SphereRec) + H.nodes4.size() * sizeof(Node4) + sizeof(int);
+    for (const HostBVH& I : H.insts)
+        n += I.nodes4.size() * sizeof(Node4) + I.recs.size() * sizeof(PrimRec) + I.spheres.size() * sizeof(SphereRec);
+    n += H.insts.size() * sizeof(DevBVH4);
+    *bytes = n;
     return PBRT_OK;
 }
 int pbrtgpu_bvh_num_nodes(const PbrtBVH* b, uint32_t* n) {

@@ -44,9 +44,9 @@ struct PbrtBVH {
     pbrt::PrimRec* d_prims = nullptr;
     pbrt::SphereRec* d_spheres = nullptr;
     pbrt::Node4* d_nodes4 = nullptr;
-    pbrt::DevBVH* d_insts = nullptr;     // per instance definition
+    pbrt::DevBVH4* d_insts = nullptr;    // per instance definition
     std::vector<void*> d_inst_bufs;      // the definitions' device arrays
-    std::vector<pbrt::DevBVH> inst_dev;  // host copy of d_insts
+    std::vector<pbrt::DevBVH4> inst_dev;  // host copy of d_insts
     int* d_status = nullptr;
     pbrt::DevBVH dev{};
     pbrt::DevBVH4 dev4{};

@@ -556,8 +556,8 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
             *err = "instance definition without shapes";
             return PBRT_ERR_INVALID_ARGUMENT;
         }
-        if (H.insts[k].depth > 64) {
-            *err = "instance definition BVH deeper than 64 levels";
+        if (H.insts[k].stack4_bound > 96) {  // kInstStack4 of the nested walk
+            *err = "instance definition BVH too deep for the nested traversal stack (96 entries)";
             return PBRT_ERR_UNSUPPORTED;
         }
     }

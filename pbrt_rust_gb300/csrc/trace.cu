@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
     int st = 0;
     DRay r;
     Traversal<STACK, INST> T;
+    T.found = false;
     auto finish = [&]() {
         if (ANY)
             occ[ray] = T.found ? 1 : 0;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __res
 // per_warp rays from the shared counter *work (zero at launch) whenever
 // their chunk is used up, so warps that drew short rays take more of them
 // and no warp is left with a long tail.
-template <int SMAX, int OVF, bool ANY, int MINB>
+template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
 __global__ void __launch_bounds__(128, MINB)
     k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ order,
                         float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status,
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(128, MINB)
     uint32_t ray = kNone;
     bool overflow = false;
     DRay r;
-    Traversal4<SMAX, OVF> T;
+    Traversal4<SMAX, OVF, INST> T;
     T.bind(smem_stack, threadIdx.x, blockDim.x);
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
@@ -327,7 +328,7 @@ static void read_variant() {
     }
 }
 
-template <int SMAX, int OVF, bool ANY, int MINB>
+template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
 static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                           float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
                                           uint32_t* work) {
@@ -338,7 +339,8 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY, MINB>, block, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY, MINB, INST>, block,
+                                                      smem);
         if (bps < 1) bps = 1;
     }
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
@@ -350,14 +352,15 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
         uint64_t chunks = (n + g_chunk - 1) / g_chunk;
         uint64_t w = chunks < warps ? chunks : warps;
         unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
-        k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ,
-                                                                                d_status, g_chunk, g_refill, work);
+        k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(
+            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work);
         return cudaGetLastError();
     }
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace4_persistent<SMAX, OVF, ANY, MINB><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status,
-                                                                            per_warp, g_refill, nullptr);
+    k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ,
+                                                                                  d_status, per_warp, g_refill,
+                                                                                  nullptr);
     return cudaGetLastError();
 }
 
@@ -488,12 +491,24 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     if (n == 0) return cudaSuccess;
     read_variant();
     if (bvh.insts) {
-        // a scene with instances: the binary-layout walk with nested
-        // instance traversal, whatever the configured kernel
+        // a scene with instances: the persistent walk with nested instance
+        // traversal (4-wide when a variant covers the stack bound),
+        // whatever the configured kernel
         const float4* r4 = reinterpret_cast<const float4*>(rays);
         float4* h4 = reinterpret_cast<float4*>(hits);
         const int stack = trace_stack_for_depth(depth);
         const bool any = occluded != nullptr;
+        const int v = wide ? wide_stack_variant(wide_bound) : 0;
+        if (v == 64)
+            return any ? launch_wide_persistent<16, 48, true, 0, true>(*wide, r4, n, order, nullptr, occluded, d_status,
+                                                                       stream, work)
+                       : launch_wide_persistent<16, 48, false, 0, true>(*wide, r4, n, order, h4, nullptr, d_status,
+                                                                        stream, work);
+        if (v == 256)
+            return any ? launch_wide_persistent<16, 240, true, 0, true>(*wide, r4, n, order, nullptr, occluded,
+                                                                        d_status, stream, work)
+                       : launch_wide_persistent<16, 240, false, 0, true>(*wide, r4, n, order, h4, nullptr, d_status,
+                                                                         stream, work);
         if (stack == 64)
             return any ? launch_persistent<64, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
                        : launch_persistent<64, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream);

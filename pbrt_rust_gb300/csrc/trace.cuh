@@ -26,6 +26,8 @@
 
 namespace pbrt {
 
+struct DevBVH4;  // trace4.cuh
+
 struct DevBVH {
     const NodePair* pairs;
     const PrimRec* prims;
@@ -34,7 +36,7 @@ struct DevBVH {
     uint32_t has_spheres;
     uint32_t n_prims;
     uint32_t empty;
-    const DevBVH* insts;  // the instance definitions' BVHs (kQuadInstance records index it)
+    const DevBVH4* insts;  // the instance definitions' BVHs (kQuadInstance records index it)
 };
 
 struct DRay {
@@ -269,16 +271,17 @@ struct TraceResult {
 // space by w2p (the record's w2o) and traced through the definition's BVH.
 // Returns the definition-local hit (prim = its refined index, -1 on a miss);
 // the caller's maxt becomes the hit's t, as ray.set_maxt(r.maxt()) does.
-// Kept out of line so that the outer traversal's registers do not grow.
+// Kept out of line so that the outer traversal's registers do not grow;
+// defined in trace4.cuh (the definitions are walked in the 4-wide layout).
 template <bool ANY>
-__device__ __noinline__ TraceResult instance_test(const DevBVH* insts, const SphereRec* s, float ox, float oy,
+__device__ __noinline__ TraceResult instance_test(const DevBVH4* insts, const SphereRec* s, float ox, float oy,
                                                   float oz, float dx, float dy, float dz, float tmin, float maxt);
 
 // One analytic primitive record: an instance (INST and kQuadInstance) or a
 // quadric (sphere_test).  *add gets the definition-local index of an
 // instance hit, 0 otherwise; *b1 / *b2 are left alone for quadrics.
 template <bool INST, bool ANY>
-__device__ __forceinline__ bool analytic_test(const SphereRec* spheres, const DevBVH* insts, uint32_t si,
+__device__ __forceinline__ bool analytic_test(const SphereRec* spheres, const DevBVH4* insts, uint32_t si,
                                               const DRay& r, float maxt, float* t, float* b1, float* b2,
                                               uint32_t* add) {
     if (INST && spheres[si].kind == kQuadInstance) {
@@ -418,23 +421,6 @@ __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, Trace
     }
     *res = T.res;
     return T.found;
-}
-
-// Definitions are at most kInstDepth levels deep (checked at creation), so
-// the nested stack never overflows.
-constexpr int kInstDepth = 64;
-
-template <bool ANY>
-__device__ __noinline__ TraceResult instance_test(const DevBVH* insts, const SphereRec* s, float ox, float oy,
-                                                  float oz, float dx, float dy, float dz, float tmin, float maxt) {
-    float o[3], d[3];
-    xf_point(s->w2o, ox, oy, oz, o);  // transform.rs:230-237: o as a point, d as a vector
-    xf_vector(s->w2o, dx, dy, dz, d);
-    const DRay ri = make_dray(make_float4(o[0], o[1], o[2], tmin), make_float4(d[0], d[1], d[2], maxt));
-    TraceResult res;
-    int status = 0;
-    traverse<kInstDepth, ANY, false>(insts[s->instance], ri, &res, &status);
-    return res;
 }
 
 }  // namespace pbrt

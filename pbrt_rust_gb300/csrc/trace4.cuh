@@ -19,8 +19,8 @@
 // [entry][thread] so a warp's accesses hit distinct banks) with an
 // optional local-memory overflow of OVF entries; the host picks a variant
 // whose SMAX + OVF covers the tree's bound (HostBVH::stack4_bound).
-// Trees holding instances are traced with the binary layout (Traversal
-// with INST), never with this one.
+// INST: the tree may hold instance records (kernels take it only for
+// scenes that have instances).
 #pragma once
 #include <stdint.h>
 
@@ -35,6 +35,7 @@ struct DevBVH4 {
     const SphereRec* spheres;
     ChildRec root;
     uint32_t empty;
+    const DevBVH4* insts;  // the instance definitions' BVHs (kQuadInstance records index it)
 };
 
 struct ChildV {
@@ -59,12 +60,30 @@ __device__ __forceinline__ ChildV ld_child(const ChildRec* c) {
     return v;
 }
 
+// The same record through two 128-bit loads.
+__device__ __forceinline__ ChildV ld_child_v4(const ChildRec* c) {
+    ChildV v;
+    const float4 a = __ldg(reinterpret_cast<const float4*>(c)), b = __ldg(reinterpret_cast<const float4*>(c) + 1);
+    v.lx = a.x;
+    v.ly = a.y;
+    v.lz = a.z;
+    v.a = __float_as_uint(a.w);
+    v.hx = b.x;
+    v.hy = b.y;
+    v.hz = b.z;
+    v.b = __float_as_uint(b.w);
+    return v;
+}
+
 template <typename T>
 __device__ __forceinline__ T sel4(uint32_t i, T x0, T x1, T x2, T x3) {
     return i == 0 ? x0 : (i == 1 ? x1 : (i == 2 ? x2 : x3));
 }
 
-template <int SMAX, int OVF>
+// LD256: fetch child records with one 256-bit load each (else two 128-bit
+// loads; the nested instance walk lives in an out-of-line function, where
+// nvcc 13.0's back end crashes on the 256-bit form).
+template <int SMAX, int OVF, bool INST = false, bool LD256 = true>
 struct Traversal4 {
     float maxt;
     uint32_t cur;
@@ -137,15 +156,17 @@ struct Traversal4 {
             float4 r2 = ldg4(pr->r2);
             uint32_t id = __float_as_uint(r0.w);
             float t, b1 = 0.0f, b2 = 0.0f;
+            uint32_t add = 0;
             bool hit;
             if (id & kSphereBit)
-                hit = sphere_test(bvh.spheres, __float_as_uint(r1.w), r, maxt, &t);
+                hit = analytic_test<INST, ANY>(bvh.spheres, bvh.insts, __float_as_uint(r1.w), r, maxt, &t, &b1, &b2,
+                                               &add);
             else
                 hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
             if (hit) {
                 maxt = t;
                 found = true;
-                res.prim = (int32_t)(id & ~kSphereBit);
+                res.prim = (int32_t)((id & ~kSphereBit) + add);
                 res.t = t;
                 res.b1 = b1;
                 res.b2 = b2;
@@ -170,8 +191,18 @@ struct Traversal4 {
     // left.
     __device__ __forceinline__ bool node(const DevBVH4& bvh, const DRay& r) {
         const Node4* nd = bvh.nodes + cur;
-        ChildV c0 = ld_child(&nd->c[0]), c1 = ld_child(&nd->c[1]);
-        ChildV c2 = ld_child(&nd->c[2]), c3 = ld_child(&nd->c[3]);
+        ChildV c0, c1, c2, c3;
+        if (LD256) {
+            c0 = ld_child(&nd->c[0]);
+            c1 = ld_child(&nd->c[1]);
+            c2 = ld_child(&nd->c[2]);
+            c3 = ld_child(&nd->c[3]);
+        } else {
+            c0 = ld_child_v4(&nd->c[0]);
+            c1 = ld_child_v4(&nd->c[1]);
+            c2 = ld_child_v4(&nd->c[2]);
+            c3 = ld_child_v4(&nd->c[3]);
+        }
         float t0, t1, t2, t3;
         bool h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
         bool h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
@@ -199,5 +230,25 @@ struct Traversal4 {
         return !overflow;
     }
 };
+
+// An instance definition's stack bound (HostBVH::stack4_bound) is at most
+// kInstStack4 (checked at creation), so the nested stack never overflows.
+constexpr int kInstStack4 = 96;
+
+template <bool ANY>
+__device__ __noinline__ TraceResult instance_test(const DevBVH4* insts, const SphereRec* s, float ox, float oy,
+                                                  float oz, float dx, float dy, float dz, float tmin, float maxt) {
+    float o[3], d[3];
+    xf_point(s->w2o, ox, oy, oz, o);  // transform.rs:230-237: o as a point, d as a vector
+    xf_vector(s->w2o, dx, dy, dz, d);
+    const DRay ri = make_dray(make_float4(o[0], o[1], o[2], tmin), make_float4(d[0], d[1], d[2], maxt));
+    const DevBVH4& B = insts[s->instance];
+    Traversal4<0, kInstStack4, false, false> T;  // the whole stack in local memory
+    if (T.start(B, ri)) {
+        while (T.template step<ANY>(B, ri)) {
+        }
+    }
+    return T.res;
+}
 
 }  // namespace pbrt

@@ -119,6 +119,12 @@ class GpuBVHAccel:
     def num_nodes(self) -> int:
         return self._u32(self._lib.pbrtgpu_bvh_num_nodes)
 
+    def device_bytes(self) -> int:
+        """Device memory the aggregate keeps resident."""
+        v = C.c_uint64()
+        abi.check(self._lib.pbrtgpu_bvh_device_bytes(self._h, C.byref(v)), self._lib)
+        return v.value
+
     def depth(self) -> int:
         return self._u32(self._lib.pbrtgpu_bvh_depth)
 

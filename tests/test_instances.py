@@ -174,3 +174,4 @@ def test_instancing_keeps_one_copy_of_each_definition():
     assert inst.num_primitives() == 2 + 64 + 2  # ground, instances, lamp
     assert copied.num_primitives() == 2 + 32 * (2000 + 2) + 32 * (1 + 2) + 2
     assert copied.num_nodes() > 100 * inst.num_nodes()
+    assert copied.device_bytes() > 25 * inst.device_bytes()
