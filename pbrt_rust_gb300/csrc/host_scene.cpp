@@ -706,6 +706,17 @@ int build_host_bvh(const PbrtShapeDesc* shapes, uint32_t n_shapes, uint32_t max_
     if (st) return st;
     fill_device_layout(H);
     fill_node4_layout(H);
+    if (!H.insts.empty()) {
+        // the 4-wide walk enters a definition with two more entries (the
+        // rest of the leaf, the exit word) on top of the scene's stack
+        uint32_t inner = 0;
+        for (const HostBVH& I : H.insts) inner = std::max(inner, I.stack4_bound);
+        H.stack4_bound += 2 + inner;
+        if (H.recs.size() >= 0x7ffffffeu) {  // leaf words stay clear of the exit word
+            *err = "too many primitives for a scene with instances";
+            return PBRT_ERR_UNSUPPORTED;
+        }
+    }
     return PBRT_OK;
 }
 

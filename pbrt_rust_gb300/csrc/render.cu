@@ -49,14 +49,14 @@ __global__ void __launch_bounds__(128) k_shadow(RenderParams P) {
     P.occluded[P.shadow_slot[q]] = occ ? 1 : 0;
 }
 
-template <int SMAX, int OVF>
+template <int SMAX, int OVF, bool INST = false>
 __global__ void __launch_bounds__(128) k_shadow4(RenderParams P) {
     extern __shared__ uint2 smem_stack[];
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= *(volatile uint32_t*)&P.counters[0]) return;
     const float4* r4 = reinterpret_cast<const float4*>(P.shadow_rays);
     DRay r = make_dray(r4[2 * (size_t)q], r4[2 * (size_t)q + 1]);
-    Traversal4<SMAX, OVF> T;
+    Traversal4<SMAX, OVF, INST> T;
     T.bind(smem_stack, threadIdx.x, blockDim.x);
     if (T.start(P.bvh4, r))
         while (T.template step<true>(P.bvh4, r)) {
@@ -101,9 +101,16 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
         uint64_t max_shadow = P.n_samples * P.n_lights;
         if (max_shadow) {
             const size_t smem = 16 * sizeof(uint2) * 128;
+            // scenes with instances: the 4-wide walk with instances when a
+            // variant covers its stack bound, else the binary one
             const bool inst = P.bvh.insts != nullptr;
+            const int iv = (inst && P.has_wide) ? wide_stack_variant(P.wide_bound) : 0;
             int wv = (P.has_wide && rk == 2 && !inst) ? wide_stack_variant(P.wide_bound) : 0;
-            if (inst && trace_stack_for_depth(P.depth) == 64)
+            if (iv == 64)
+                k_shadow4<16, 48, true><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
+            else if (iv == 256)
+                k_shadow4<16, 240, true><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
+            else if (inst && trace_stack_for_depth(P.depth) == 64)
                 k_shadow<64, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
             else if (inst)
                 k_shadow<256, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(128)
         if (nblocked && (4 * nblocked >= nbusy || nkept == nbusy)) {
             // leaf round: every kept leaf is tested now
             if (busy && kept != kNone) {
-                const bool stop = T.template leaf<ANY>(bvh, r, kept);
+                const bool stop = T.template leaf<ANY>(bvh, r, kept) == 1;
                 kept = kNone;
                 if (stop || T.overflow) finish();
             }

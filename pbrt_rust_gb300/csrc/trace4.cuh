@@ -80,11 +80,43 @@ __device__ __forceinline__ T sel4(uint32_t i, T x0, T x1, T x2, T x3) {
     return i == 0 ? x0 : (i == 1 ? x1 : (i == 2 ? x2 : x3));
 }
 
+// Stack word that ends the walk of an instance definition (never a leaf:
+// primitive offsets stay below 0x7ffffffe).
+constexpr uint32_t kExitInst = 0xfffffffeu;
+
 // LD256: fetch child records with one 256-bit load each (else two 128-bit
-// loads; the nested instance walk lives in an out-of-line function, where
-// nvcc 13.0's back end crashes on the 256-bit form).
+// loads; the nested instance walk of the binary kernels lives in an
+// out-of-line function, where nvcc 13.0's back end crashes on the 256-bit
+// form).
+//
+// INST: the tree may hold instance records.  An instance is walked in the
+// same loop as the scene's tree (TransformedPrimitive::intersect,
+// transformed.rs:35-56): when its leaf entry is reached and the
+// primitive-space ray w2p(ray) - o as a point, d as a vector, mint and the
+// current maxt kept - passes the definition's root box, the walk pushes the
+// rest of the leaf and an exit word (both with entry distance -inf, so they
+// are always taken) and continues in the definition's tree with that ray;
+// popping the exit word restores the world ray and the scene's tree.  The
+// definition is thus searched completely, in the reference's order, before
+// the leaf's next primitive, and the shared maxt is the reference's
+// ray.set_maxt.  Hits inside report the instance's first id + the
+// definition-local index.  The stack bound of such a tree includes the
+// largest definition's bound + 2 (HostBVH::stack4_bound).
+// INST walks' extra state: the arrays of the tree being walked, the world
+// ray while inside an instance, and the instance's first id (0 outside).
+template <bool INST>
+struct InstWalk {
+    const Node4* nodes_;
+    const PrimRec* prims_;
+    const SphereRec* spheres_;
+    float wox_, woy_, woz_, wdx_, wdy_, wdz_;
+    uint32_t base_;
+};
+template <>
+struct InstWalk<false> {};
+
 template <int SMAX, int OVF, bool INST = false, bool LD256 = true>
-struct Traversal4 {
+struct Traversal4 : InstWalk<INST> {
     float maxt;
     uint32_t cur;
     int sp;
@@ -100,6 +132,25 @@ struct Traversal4 {
         stride = nthreads;
     }
 
+    __device__ __forceinline__ const Node4* node_base(const DevBVH4& bvh) const {
+        if constexpr (INST)
+            return this->nodes_;
+        else
+            return bvh.nodes;
+    }
+    __device__ __forceinline__ const PrimRec* prim_base(const DevBVH4& bvh) const {
+        if constexpr (INST)
+            return this->prims_;
+        else
+            return bvh.prims;
+    }
+    __device__ __forceinline__ const SphereRec* sphere_base(const DevBVH4& bvh) const {
+        if constexpr (INST)
+            return this->spheres_;
+        else
+            return bvh.spheres;
+    }
+
     __device__ __forceinline__ bool start(const DevBVH4& bvh, const DRay& r) {
         maxt = r.tmax;
         found = false;
@@ -109,6 +160,12 @@ struct Traversal4 {
         res.t = 0.0f;
         res.b1 = 0.0f;
         res.b2 = 0.0f;
+        if constexpr (INST) {
+            this->nodes_ = bvh.nodes;
+            this->prims_ = bvh.prims;
+            this->spheres_ = bvh.spheres;
+            this->base_ = 0;
+        }
         if (bvh.empty) return false;
         float tr;
         const ChildRec& R = bvh.root;
@@ -144,43 +201,108 @@ struct Traversal4 {
         return false;
     }
 
+    // INST: starts the walk of instance record S (first id `first`) if the
+    // primitive-space ray hits its definition's root box; `resume` is the
+    // leaf word of the rest of the current leaf (0: none).
+    template <class R>
+    __device__ __forceinline__ bool enter(const DevBVH4& bvh, R& r, const SphereRec* S, uint32_t first,
+                                          uint32_t resume) {
+        float o[3], d[3];
+        xf_point(S->w2o, r.ox, r.oy, r.oz, o);  // transform.rs:230-237
+        xf_vector(S->w2o, r.dx, r.dy, r.dz, d);
+        const DRay ri = make_dray(make_float4(o[0], o[1], o[2], r.tmin), make_float4(d[0], d[1], d[2], maxt));
+        const DevBVH4& D = bvh.insts[S->instance];
+        float tr;
+        const ChildRec& Rt = D.root;
+        if (D.empty || !slab(Rt.lo_x, Rt.lo_y, Rt.lo_z, Rt.hi_x, Rt.hi_y, Rt.hi_z, ri, maxt, &tr)) return false;
+        if (resume) push(resume, __int_as_float(0xff800000));  // -inf: always taken
+        push(kExitInst, __int_as_float(0xff800000));
+        this->wox_ = r.ox;
+        this->woy_ = r.oy;
+        this->woz_ = r.oz;
+        this->wdx_ = r.dx;
+        this->wdy_ = r.dy;
+        this->wdz_ = r.dz;
+        r = ri;
+        this->nodes_ = D.nodes;
+        this->prims_ = D.prims;
+        this->spheres_ = D.spheres;
+        this->base_ = first;
+        cur = Rt.a;
+        return !overflow;
+    }
+
+    // INST: back to the scene's tree and the world ray (make_dray gives the
+    // same 1/d and signs as at the start).
+    template <class R>
+    __device__ __forceinline__ void leave(const DevBVH4& bvh, R& r) {
+        r = make_dray(make_float4(this->wox_, this->woy_, this->woz_, r.tmin),
+                      make_float4(this->wdx_, this->wdy_, this->wdz_, r.tmax));
+        this->nodes_ = bvh.nodes;
+        this->prims_ = bvh.prims;
+        this->spheres_ = bvh.spheres;
+        this->base_ = 0;
+    }
+
     // Tests the primitives of leaf `ref` (a kNode4Leaf child word) in
-    // order; true if ANY and one was hit.
-    template <bool ANY>
-    __device__ __forceinline__ bool leaf(const DevBVH4& bvh, const DRay& r, uint32_t ref) {
+    // order.  Returns 0 when the leaf is done, 1 when ANY and a primitive
+    // was hit, 2 when an instance walk was entered (`cur` set).
+    template <bool ANY, class R>
+    __device__ __forceinline__ int leaf(const DevBVH4& bvh, R& r, uint32_t ref) {
         uint32_t off = ref & ~kNode4Leaf;
         for (;;) {
-            const PrimRec* pr = bvh.prims + off;
+            const PrimRec* pr = prim_base(bvh) + off;
             float4 r0 = ldg4(pr->r0);
             float4 r1 = ldg4(pr->r1);
             float4 r2 = ldg4(pr->r2);
             uint32_t id = __float_as_uint(r0.w);
+            const bool last = (__float_as_uint(r2.w) & kPrimLastBit) != 0;
             float t, b1 = 0.0f, b2 = 0.0f;
-            uint32_t add = 0;
             bool hit;
-            if (id & kSphereBit)
-                hit = analytic_test<INST, ANY>(bvh.spheres, bvh.insts, __float_as_uint(r1.w), r, maxt, &t, &b1, &b2,
-                                               &add);
-            else
+            if (id & kSphereBit) {
+                const uint32_t si = __float_as_uint(r1.w);
+                if constexpr (INST) {
+                    const SphereRec* S = sphere_base(bvh) + si;
+                    if (S->kind == kQuadInstance) {  // only in the scene's tree: definitions hold none
+                        if (enter(bvh, r, S, id & ~kSphereBit, last ? 0u : (kNode4Leaf | (off + 1)))) return 2;
+                        if (last) return 0;
+                        ++off;
+                        continue;
+                    }
+                }
+                hit = sphere_test(sphere_base(bvh), si, r, maxt, &t);
+            } else {
                 hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
+            }
             if (hit) {
                 maxt = t;
                 found = true;
-                res.prim = (int32_t)((id & ~kSphereBit) + add);
+                if constexpr (INST)
+                    res.prim = (int32_t)(this->base_ + (id & ~kSphereBit));
+                else
+                    res.prim = (int32_t)(id & ~kSphereBit);
                 res.t = t;
                 res.b1 = b1;
                 res.b2 = b2;
-                if (ANY) return true;
+                if (ANY) return 1;
             }
-            if (__float_as_uint(r2.w) & kPrimLastBit) return false;
+            if (last) return 0;
             ++off;
         }
     }
 
-    template <bool ANY>
-    __device__ __forceinline__ bool step(const DevBVH4& bvh, const DRay& r) {
+    template <bool ANY, class R>
+    __device__ __forceinline__ bool step(const DevBVH4& bvh, R& r) {
+        if constexpr (INST) {
+            if (cur == kExitInst) {
+                leave(bvh, r);
+                return pop();
+            }
+        }
         if (cur & kNode4Leaf) {
-            if (leaf<ANY>(bvh, r, cur)) return false;
+            const int st = leaf<ANY>(bvh, r, cur);
+            if (st == 1) return false;
+            if (INST && st == 2) return !overflow;
             return pop();
         }
         return node(bvh, r);
@@ -190,7 +312,7 @@ struct Traversal4 {
     // next node or leaf in the reference's order; false once nothing is
     // left.
     __device__ __forceinline__ bool node(const DevBVH4& bvh, const DRay& r) {
-        const Node4* nd = bvh.nodes + cur;
+        const Node4* nd = node_base(bvh) + cur;
         ChildV c0, c1, c2, c3;
         if (LD256) {
             c0 = ld_child(&nd->c[0]);
@@ -241,7 +363,7 @@ __device__ __noinline__ TraceResult instance_test(const DevBVH4* insts, const Sp
     float o[3], d[3];
     xf_point(s->w2o, ox, oy, oz, o);  // transform.rs:230-237: o as a point, d as a vector
     xf_vector(s->w2o, dx, dy, dz, d);
-    const DRay ri = make_dray(make_float4(o[0], o[1], o[2], tmin), make_float4(d[0], d[1], d[2], maxt));
+    DRay ri = make_dray(make_float4(o[0], o[1], o[2], tmin), make_float4(d[0], d[1], d[2], maxt));
     const DevBVH4& B = insts[s->instance];
     Traversal4<0, kInstStack4, false, false> T;  // the whole stack in local memory
     if (T.start(B, ri)) {
