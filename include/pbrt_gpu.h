@@ -288,7 +288,7 @@ enum {
 typedef struct PbrtTraceConfig {
     int32_t kernel;         /* PBRT_TRACE_*: pbrtgpu_intersect / intersect_p batches */
     uint32_t refill;        /* persistent kernels: refill a warp when this many lanes idle */
-    uint32_t min_blocks;    /* 4-wide persistent kernel: 0, or 8 / 9 resident 128-thread
+    uint32_t min_blocks;    /* 4-wide persistent kernel: 0, or 7 / 8 / 9 resident 128-thread
                                blocks per SM requested (fewer registers per thread) */
     int32_t render_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and shadow
                                rays inside pbrtgpu_render (coherent batches) */

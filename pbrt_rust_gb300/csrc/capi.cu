@@ -432,7 +432,7 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t ca
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg) {
     if (!cfg || set_trace_config(*cfg))
         return set_error(PBRT_ERR_INVALID_ARGUMENT,
-                         "trace config: kernel 0..4, refill 1..32, min_blocks 0/8/9, render_kernel 0 or 2, "
+                         "trace config: kernel 0..4, refill 1..32, min_blocks 0/7/8/9, render_kernel 0 or 2, "
                          "reorder 0/1");
     return PBRT_OK;
 }

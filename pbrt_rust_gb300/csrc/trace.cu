@@ -313,7 +313,7 @@ static void read_variant() {
     }
     if (const char* m = getenv("PBRT_TRACE_MINB")) {
         int x = atoi(m);
-        if (x == 0 || x == 8 || x == 9) g_min_blocks = (unsigned)x;
+        if (x == 0 || x == 7 || x == 8 || x == 9) g_min_blocks = (unsigned)x;
     }
     if (const char* v = getenv("PBRT_TRACE_CHUNK")) {
         int x = atoi(v);
@@ -405,6 +405,8 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
         k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status);
         return cudaGetLastError();
     }
+    if (g_min_blocks == 7)
+        return launch_wide_persistent<SMAX, OVF, ANY, 7>(bvh, r4, n, order, h4, occ, d_status, stream, work);
     if (g_min_blocks == 8)
         return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, order, h4, occ, d_status, stream, work);
     if (g_min_blocks == 9)
@@ -414,7 +416,7 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
 
 int set_trace_config(const PbrtTraceConfig& c) {
     if (c.kernel < kVariantPairPlain || c.kernel > kVariantWideSpeculative || c.refill < 1 || c.refill > 32) return 1;
-    if (!(c.min_blocks == 0 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
+    if (!(c.min_blocks == 0 || c.min_blocks == 7 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
     if (c.render_kernel != kVariantPairPlain && c.render_kernel != kVariantWidePlain) return 1;
     if (c.reorder > 1) return 1;
     if (!(c.chunk == 0 || (c.chunk >= 32 && c.chunk <= 4096 && c.chunk % 32 == 0))) return 1;

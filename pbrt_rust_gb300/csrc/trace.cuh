@@ -43,8 +43,15 @@ struct DRay {
     float ox, oy, oz, tmin;
     float dx, dy, dz, tmax;
     float ix, iy, iz;  // 1/d
-    uint32_t neg;      // bit i: inv_dir[i] < 0 (bvh.rs:383)
+    uint32_t neg;      // bit i: inv_dir[i] < 0 (bvh.rs:383); kRayClean
 };
+
+// DRay::neg bit: origin and 1/d finite, tmin and tmax not NaN (slab_clean).
+constexpr uint32_t kRayClean = 8u;
+
+__device__ __forceinline__ bool finite3(float a, float b, float c) {
+    return fabsf(a) <= 3.402823466e38f && fabsf(b) <= 3.402823466e38f && fabsf(c) <= 3.402823466e38f;
+}
 
 __device__ __forceinline__ DRay make_dray(float4 a, float4 b) {
     DRay r;
@@ -60,6 +67,8 @@ __device__ __forceinline__ DRay make_dray(float4 a, float4 b) {
     r.iy = 1.0f / r.dy;
     r.iz = 1.0f / r.dz;
     r.neg = (r.ix < 0.0f ? 1u : 0u) | (r.iy < 0.0f ? 2u : 0u) | (r.iz < 0.0f ? 4u : 0u);
+    if (finite3(r.ix, r.iy, r.iz) && finite3(r.ox, r.oy, r.oz) && r.tmin == r.tmin && r.tmax == r.tmax)
+        r.neg |= kRayClean;
     return r;
 }
 
@@ -83,6 +92,36 @@ __device__ __forceinline__ bool slab(float lox, float loy, float loz, float hix,
     tf = ta > tb ? ta : tb;
     t0 = fmaxf(tn, t0);
     t1 = fminf(tf, t1);
+    *t_enter = t0;
+    return !(t0 > t1);
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// slab() for a kRayClean ray.  Its products (lo - o) * (1/d) can be NaN
+// only where a box coordinate is NaN, and a box built from unions and
+// transforms of the same points has lo NaN exactly where hi is NaN.  So
+// the reference's "swap if tnear > tfar" is min/max, an all-NaN axis drops
+// out of min/max as it drops out of the reference's comparisons, and the
+// four entry bounds (tmin and the three near planes) and four exit bounds
+// combine in any order: the same t0 and the same decision, in fewer
+// instructions.
+__device__ __forceinline__ bool slab_clean(float lox, float loy, float loz, float hix, float hiy, float hiz,
+                                           const DRay& r, float maxt, float* t_enter) {
+    const float ax = (lox - r.ox) * r.ix, bx = (hix - r.ox) * r.ix;
+    const float ay = (loy - r.oy) * r.iy, by = (hiy - r.oy) * r.iy;
+    const float az = (loz - r.oz) * r.iz, bz = (hiz - r.oz) * r.iz;
+    const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), r.tmin));
+    const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), maxt));
     *t_enter = t0;
     return !(t0 > t1);
 }
@@ -367,8 +406,14 @@ struct Traversal {
             float4 c0a = ldg4(&np->c[0].lo_x), c0b = ldg4(&np->c[0].hi_x);
             float4 c1a = ldg4(&np->c[1].lo_x), c1b = ldg4(&np->c[1].hi_x);
             float t0, t1;
-            bool h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
-            bool h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+            bool h0, h1;
+            if (r.neg & kRayClean) {
+                h0 = slab_clean(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
+                h1 = slab_clean(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+            } else {
+                h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
+                h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+            }
             // Near child: child1 unless dir_is_neg[axis] (bvh.rs:409-415).
             bool swap = (r.neg >> b) & 1u;
             uint32_t na = swap ? __float_as_uint(c1a.w) : __float_as_uint(c0a.w);

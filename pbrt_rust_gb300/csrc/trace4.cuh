@@ -75,9 +75,17 @@ __device__ __forceinline__ ChildV ld_child_v4(const ChildRec* c) {
     return v;
 }
 
-template <typename T>
-__device__ __forceinline__ T sel4(uint32_t i, T x0, T x1, T x2, T x3) {
-    return i == 0 ? x0 : (i == 1 ? x1 : (i == 2 ? x2 : x3));
+// Swaps two (child word, hit, entry distance) entries when c.
+__device__ __forceinline__ void cswap(bool c, uint32_t& a, uint32_t& b, bool& ha, bool& hb, float& ta, float& tb) {
+    const uint32_t x = c ? b : a, y = c ? a : b;
+    const bool hx = c ? hb : ha, hy = c ? ha : hb;
+    const float tx = c ? tb : ta, ty = c ? ta : tb;
+    a = x;
+    b = y;
+    ha = hx;
+    hb = hy;
+    ta = tx;
+    tb = ty;
 }
 
 // Stack word that ends the walk of an instance definition (never a leaf:
@@ -326,29 +334,35 @@ struct Traversal4 : InstWalk<INST> {
             c3 = ld_child_v4(&nd->c[3]);
         }
         float t0, t1, t2, t3;
-        bool h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
-        bool h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
-        bool h2 = c2.a != kNode4Empty && slab(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
-        bool h3 = c3.a != kNode4Empty && slab(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+        bool h0, h1, h2, h3;
+        if (r.neg & kRayClean) {
+            h0 = c0.a != kNode4Empty && slab_clean(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
+            h1 = c1.a != kNode4Empty && slab_clean(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
+            h2 = c2.a != kNode4Empty && slab_clean(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
+            h3 = c3.a != kNode4Empty && slab_clean(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+        } else {
+            h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
+            h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
+            h2 = c2.a != kNode4Empty && slab(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
+            h3 = c3.a != kNode4Empty && slab(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+        }
         if (!(h0 | h1 | h2 | h3)) return pop();
         const uint32_t meta = c0.b;
         const bool sN = (r.neg >> (meta & 3u)) & 1u;
         const bool sL = (r.neg >> ((meta >> 2) & 3u)) & 1u;
         const bool sR = (r.neg >> ((meta >> 4) & 3u)) & 1u;
-        // slot index at each visit position (bvh.rs:409-415 applied at N,
-        // then at the child visited first, then at the other one)
-        const uint32_t la = sL ? 1u : 0u, lb = sL ? 0u : 1u, ra = sR ? 3u : 2u, rb = sR ? 2u : 3u;
-        const uint32_t o0 = sN ? ra : la, o1 = sN ? rb : lb, o2 = sN ? la : ra, o3 = sN ? lb : rb;
-        const bool q0 = sel4(o0, h0, h1, h2, h3), q1 = sel4(o1, h0, h1, h2, h3);
-        const bool q2 = sel4(o2, h0, h1, h2, h3), q3 = sel4(o3, h0, h1, h2, h3);
-        const uint32_t p0 = sel4(o0, c0.a, c1.a, c2.a, c3.a), p1 = sel4(o1, c0.a, c1.a, c2.a, c3.a);
-        const uint32_t p2 = sel4(o2, c0.a, c1.a, c2.a, c3.a), p3 = sel4(o3, c0.a, c1.a, c2.a, c3.a);
-        const float u1 = sel4(o1, t0, t1, t2, t3), u2 = sel4(o2, t0, t1, t2, t3), u3 = sel4(o3, t0, t1, t2, t3);
-        const int first = q0 ? 0 : (q1 ? 1 : (q2 ? 2 : 3));
-        if (q3 && first < 3) push(p3, u3);
-        if (q2 && first < 2) push(p2, u2);
-        if (q1 && first < 1) push(p1, u1);
-        cur = first == 0 ? p0 : (first == 1 ? p1 : (first == 2 ? p2 : p3));
+        // into visit order (bvh.rs:409-415): each child's pair of children
+        // by that child's axis sign, then the two pairs by N's
+        uint32_t a0 = c0.a, a1 = c1.a, a2 = c2.a, a3 = c3.a;
+        cswap(sL, a0, a1, h0, h1, t0, t1);
+        cswap(sR, a2, a3, h2, h3, t2, t3);
+        cswap(sN, a0, a2, h0, h2, t0, t2);
+        cswap(sN, a1, a3, h1, h3, t1, t3);
+        const int first = h0 ? 0 : (h1 ? 1 : (h2 ? 2 : 3));
+        if (h3 && first < 3) push(a3, t3);
+        if (h2 && first < 2) push(a2, t2);
+        if (h1 && first < 1) push(a1, t1);
+        cur = first == 0 ? a0 : (first == 1 ? a1 : (first == 2 ? a2 : a3));
         return !overflow;
     }
 };
