@@ -290,8 +290,9 @@ typedef struct PbrtTraceConfig {
     uint32_t refill;        /* persistent kernels: refill a warp when this many lanes idle */
     uint32_t min_blocks;    /* 4-wide persistent kernel: 0, or 7 / 8 / 9 resident 128-thread
                                blocks per SM requested (fewer registers per thread) */
-    int32_t render_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and shadow
-                               rays inside pbrtgpu_render (coherent batches) */
+    int32_t render_kernel;  /* PBRT_TRACE_*: camera rays inside pbrtgpu_render; shadow
+                               rays take the 4-wide kernel with a 4-wide choice, else
+                               the binary one */
     uint32_t reorder;       /* 1: pbrtgpu_intersect / intersect_p batches of 32768 rays
                                or more are binned by direction and origin before
                                traversal (same results, more coherent warps) */

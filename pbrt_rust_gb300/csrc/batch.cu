@@ -22,6 +22,7 @@ namespace pbrt {
 
 cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool inst,
                                uint32_t cover_pair, uint32_t cover_wide, int sms, cudaStream_t s);
+cudaError_t launch_batch_replay(const BatchArgs& A, const BatchTuning& T, int sms, cudaStream_t s);
 
 namespace {
 
@@ -112,6 +113,8 @@ cudaError_t launch_batch_stages(const BatchArgs& A, const BatchTuning& T, bool m
     const bool b256 = T.block == 256;
     if ((e = b256 ? stage(kb_generate<256>) : stage(kb_generate<128>)) != cudaSuccess) return e;
     if ((e = launch_batch_trace(A, T, false, mixed, inst, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;
+    ++*launches;
+    if ((e = launch_batch_replay(A, T, sms, s)) != cudaSuccess) return e;
     ++*launches;
     if ((e = b256 ? stage(kb_shade<256>) : stage(kb_shade<128>)) != cudaSuccess) return e;
     if ((e = launch_batch_trace(A, T, true, false, inst, cover_pair, cover_wide, sms, s)) != cudaSuccess) return e;

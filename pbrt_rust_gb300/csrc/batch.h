@@ -41,6 +41,7 @@ enum {
     kCtrShadowCount = 0,  // shadow rays queued by shade
     kCtrExtendWork = 1,   // work counter of the extend kernel
     kCtrShadowWork = 2,   // work counter of the shadow kernel
+    kCtrReplay = 3,       // some closest hit needs the exact replay (Traversal in trace.cuh)
     kCtrWords = 8         // counters per slot; slot 0 = batch, slot j+1 = job j
 };
 

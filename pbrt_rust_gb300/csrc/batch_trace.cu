@@ -88,6 +88,7 @@ struct Walker<true, SMAX, OVF> {
     }
     __device__ __forceinline__ int failure() const { return T.overflow ? 6 : 0; }
     __device__ __forceinline__ bool found() const { return T.found; }
+    __device__ __forceinline__ bool nan_hit() const { return T.nan_hit; }
     __device__ __forceinline__ const TraceResult& res() const { return T.res; }
 };
 
@@ -110,6 +111,7 @@ struct Walker<false, STACK, INST> {
     }
     __device__ __forceinline__ int failure() const { return st; }
     __device__ __forceinline__ bool found() const { return T.found; }
+    __device__ __forceinline__ bool nan_hit() const { return T.nan_hit; }
     __device__ __forceinline__ const TraceResult& res() const { return T.res; }
 };
 
@@ -138,6 +140,9 @@ __global__ void __launch_bounds__(BLOCK) kb_trace(BatchArgs A) {
             J.P.occluded[__ldg(A.q_slot + item)] = K.found() ? 1 : 0;
         } else if (any) {
             J.occ[item] = K.found() ? 1 : 0;
+        } else if (K.nan_hit()) {  // rewritten by the replay stage
+            J.hits[item] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+            A.counters[kCtrReplay] = 1u;
         } else {
             const TraceResult& R = K.res();
             J.hits[item] = make_float4(__int_as_float(R.prim), R.t, R.b1, R.b2);
@@ -179,6 +184,30 @@ __global__ void __launch_bounds__(BLOCK) kb_trace(BatchArgs A) {
     }
 }
 
+// The exact replay of the closest hits the extend stage marked (see
+// Traversal in trace.cuh): the binary walk with instances allowed; returns
+// at once when nothing was marked.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) kb_replay(BatchArgs A) {
+    if (*(const volatile uint32_t*)(A.counters + kCtrReplay) == 0u) return;
+    const uint64_t n = A.hdr->rays;
+    const uint32_t nj = A.hdr->n_jobs;
+    Cursor c{0, 1, 0};
+    for (uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; g < n; g += (uint64_t)gridDim.x * BLOCK) {
+        const uint32_t j = locate(A.off_ray, nj, g, c);
+        const JobRec& J = A.jobs[j];
+        if (J.any) continue;
+        const uint64_t item = g - c.lo;
+        if (__float_as_int(J.hits[item].x) != kReplayMark) continue;
+        const DRay r = make_dray(__ldg(J.rays + 2 * item), __ldg(J.rays + 2 * item + 1));
+        TraceResult res;
+        int st = 0;
+        traverse<256, false, true, true>(J.P.bvh, r, &res, &st);
+        if (st) atomicMax((int*)(J.P.counters + 2), st);
+        J.hits[item] = make_float4(__int_as_float(res.prim), res.t, res.b1, res.b2);
+    }
+}
+
 template <int BLOCK, bool SHADOW, bool WIDE, int S1, int S2, int MODE>
 cudaError_t go(const BatchArgs& A, int sms, cudaStream_t s) {
     static int bps = 0;
@@ -217,6 +246,14 @@ cudaError_t pick_block(const BatchArgs& A, const BatchTuning& T, bool shadow, bo
 }
 
 }  // namespace
+
+cudaError_t launch_batch_replay(const BatchArgs& A, const BatchTuning& T, int sms, cudaStream_t s) {
+    if (T.block == 256)
+        kb_replay<256><<<(unsigned)(sms * 2), 256, 0, s>>>(A);
+    else
+        kb_replay<128><<<(unsigned)(sms * 4), 128, 0, s>>>(A);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_batch_trace(const BatchArgs& A, const BatchTuning& T, bool shadow, bool mixed, bool inst,
                                uint32_t cover_pair, uint32_t cover_wide, int sms, cudaStream_t s) {

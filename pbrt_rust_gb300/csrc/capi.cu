@@ -188,20 +188,18 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
     int st;
     const bool reorder = trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
     const bool chunked = trace_chunk() != 0;
-    if (reorder || chunked) {
-        // [256 B: chunk counter][permutation scratch]
-        cudaMemPool_t pool;
-        if ((st = scratch_pool(b->device, &pool))) return st;
-        const size_t bytes = 256 + (reorder ? ray_order_scratch_bytes(n) : 0);
-        if ((st = cuda_status(cudaMallocFromPoolAsync(&scratch, bytes, pool, s), "cudaMallocFromPoolAsync")))
-            return st;
-        work = static_cast<uint32_t*>(scratch);
-        if ((st = cuda_status(cudaMemsetAsync(work, 0, sizeof(uint32_t), s), "cudaMemsetAsync"))) {
-            cudaFreeAsync(scratch, s);
-            return st;
-        }
-        if (!chunked) work = nullptr;
+    // [256 B: chunk counter, replay flag][permutation scratch]
+    cudaMemPool_t pool;
+    if ((st = scratch_pool(b->device, &pool))) return st;
+    const size_t bytes = 256 + (reorder ? ray_order_scratch_bytes(n) : 0);
+    if ((st = cuda_status(cudaMallocFromPoolAsync(&scratch, bytes, pool, s), "cudaMallocFromPoolAsync"))) return st;
+    work = static_cast<uint32_t*>(scratch);
+    uint32_t* replay = work + 1;
+    if ((st = cuda_status(cudaMemsetAsync(work, 0, 2 * sizeof(uint32_t), s), "cudaMemsetAsync"))) {
+        cudaFreeAsync(scratch, s);
+        return st;
     }
+    if (!chunked) work = nullptr;
     if (reorder) {
         const Box& wb = b->host.nodes[0].box;
         ReorderBounds B;
@@ -221,9 +219,9 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
         order = ord;
     }
     st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, d_hits, d_occ, b->d_status, s, wide_of(b),
-                                  b->host.stack4_bound, -1, order, work),
+                                  b->host.stack4_bound, -1, order, work, replay),
                      "trace launch");
-    if (scratch) cudaFreeAsync(scratch, s);
+    cudaFreeAsync(scratch, s);
     return st;
 }
 
@@ -432,7 +430,7 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* b, uint32_t* out, uint32_t ca
 int pbrtgpu_set_trace_config(const PbrtTraceConfig* cfg) {
     if (!cfg || set_trace_config(*cfg))
         return set_error(PBRT_ERR_INVALID_ARGUMENT,
-                         "trace config: kernel 0..4, refill 1..32, min_blocks 0/7/8/9, render_kernel 0 or 2, "
+                         "trace config: kernel 0..4, refill 1..32, min_blocks 0/7/8/9, render_kernel 0..4, "
                          "reorder 0/1");
     return PBRT_OK;
 }

@@ -20,11 +20,14 @@ int trace_stack_for_depth(uint32_t depth);
 // `kernel` >= 0 overrides the process-wide choice (PBRT_TRACE_*).  With
 // `order` (a permutation of [0, n)) the kernels take ray order[j] as their
 // j-th ray; hits still land at each ray's own index.  `work` is the 4-wide
-// persistent kernel's chunk counter (see trace_chunk).
+// persistent kernel's chunk counter (see trace_chunk).  `replay` (closest
+// hit: required; a device word, zero at launch) flags that some ray's walk
+// accepted a NaN distance; a replay kernel queued after the traversal then
+// rewrites those rays' hits by the exact walk (see Traversal in trace.cuh).
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide = nullptr,
                          uint32_t wide_bound = 0, int kernel = -1, const uint32_t* order = nullptr,
-                         uint32_t* work = nullptr);
+                         uint32_t* work = nullptr, uint32_t* replay = nullptr);
 // Process-wide traversal configuration (PBRT_TRACE_* and the environment
 // variables of pbrt_gpu.h); set returns 0 on success, 1 for invalid fields.
 int set_trace_config(const PbrtTraceConfig& cfg);

@@ -94,7 +94,8 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
         // ray keeps them together in a warp
         const int rk = render_trace_kernel();
         e = launch_trace(P.bvh, P.depth, P.rays, (uint32_t)P.n_samples, reinterpret_cast<PbrtHit*>(P.hits), nullptr,
-                         (int*)&P.counters[2], s, P.has_wide ? &P.bvh4 : nullptr, P.wide_bound, rk);
+                         (int*)&P.counters[2], s, P.has_wide ? &P.bvh4 : nullptr, P.wide_bound, rk, nullptr, nullptr,
+                         &P.counters[3]);
         if (e != cudaSuccess) return e;
         k_shade<<<blocks_for(P.n_samples, 128), 128, 0, s>>>(P);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -105,7 +106,8 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
             // variant covers its stack bound, else the binary one
             const bool inst = P.bvh.insts != nullptr;
             const int iv = (inst && P.has_wide) ? wide_stack_variant(P.wide_bound) : 0;
-            int wv = (P.has_wide && rk == 2 && !inst) ? wide_stack_variant(P.wide_bound) : 0;
+            const bool wide_rk = rk == PBRT_TRACE_WIDE || rk == PBRT_TRACE_WIDE_PERSISTENT || rk == PBRT_TRACE_WIDE_SPECULATIVE;
+            int wv = (P.has_wide && wide_rk && !inst) ? wide_stack_variant(P.wide_bound) : 0;
             if (iv == 64)
                 k_shadow4<16, 48, true><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
             else if (iv == 256)

@@ -103,7 +103,7 @@ struct RenderParams {
     float4* L;          // per sample radiance
     PbrtRay* shadow_rays;
     uint32_t* shadow_slot;
-    uint32_t* counters;  // [0] shadow rays, [1] NaN samples
+    uint32_t* counters;  // [0] shadow rays, [1] NaN samples, [2] status, [3] replay flag (zero at launch)
     uint8_t* occluded;   // per (sample, light)
     float* rgb;          // film output
 };

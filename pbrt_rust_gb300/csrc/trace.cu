@@ -14,10 +14,11 @@ namespace pbrt {
 // One thread per ray.  Rays are two float4 loads (32 B, coalesced); a
 // closest hit is one 16-byte store, an any-hit answer one byte.
 template <int STACK, bool ANY>
-__global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128) k_trace(const __grid_constant__ DevBVH bvh, const float4* __restrict__ rays,
+                                               uint32_t n,
                                                const uint32_t* __restrict__ order, float4* __restrict__ hits,
-    uint8_t* __restrict__ occ,
-                                               int* __restrict__ status) {
+                                               uint8_t* __restrict__ occ, int* __restrict__ status,
+                                               uint32_t* __restrict__ replay) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (order) i = __ldg(order + i);
@@ -25,12 +26,17 @@ __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restr
     DRay r = make_dray(a, b);
     TraceResult res;
     int st = 0;
-    bool found = traverse<STACK, ANY>(bvh, r, &res, &st);
+    bool nan_hit = false;
+    bool found = traverse<STACK, ANY>(bvh, r, &res, &st, &nan_hit);
     if (st) atomicMax(status, st);
-    if (ANY)
+    if (ANY) {
         occ[i] = found ? 1 : 0;
-    else
+    } else if (nan_hit) {
+        hits[i] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+        *replay = 1u;
+    } else {
         hits[i] = make_float4(__int_as_float(res.prim), res.t, res.b1, res.b2);
+    }
 }
 
 // Persistent warps: the grid holds exactly the resident warps; each warp
@@ -40,11 +46,12 @@ __global__ void __launch_bounds__(128) k_trace(DevBVH bvh, const float4* __restr
 // longest one finishes.  Each ray's own traversal is unchanged, so results
 // are identical to k_trace.
 template <int STACK, bool ANY, bool INST = false>
-__global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128) k_trace_persistent(const __grid_constant__ DevBVH bvh,
+                                                          const float4* __restrict__ rays, uint32_t n,
                                                           const uint32_t* __restrict__ order, float4* __restrict__ hits,
-    uint8_t* __restrict__ occ,
-                                                          int* __restrict__ status, uint32_t per_warp,
-                                                          uint32_t refill) {
+                                                          uint8_t* __restrict__ occ, int* __restrict__ status,
+                                                          uint32_t per_warp, uint32_t refill,
+                                                          uint32_t* __restrict__ replay) {
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint64_t next = warp * per_warp;
@@ -56,10 +63,16 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
     Traversal<STACK, INST> T;
     T.found = false;
     auto finish = [&]() {
-        if (ANY)
+        if (ANY) {
             occ[ray] = T.found ? 1 : 0;
-        else
-            hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        } else {
+            if (T.nan_hit) {
+                hits[ray] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+                *replay = 1u;
+            } else {
+                hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+            }
+        }
         ray = kNone;
     };
     for (;;) {
@@ -88,10 +101,11 @@ __global__ void __launch_bounds__(128) k_trace_persistent(DevBVH bvh, const floa
 
 // 4-wide traversal, one thread per ray.
 template <int SMAX, int OVF, bool ANY>
-__global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128) k_trace4(const __grid_constant__ DevBVH4 bvh, const float4* __restrict__ rays,
+                                                uint32_t n,
                                                 const uint32_t* __restrict__ order, float4* __restrict__ hits,
-    uint8_t* __restrict__ occ,
-                                                int* __restrict__ status) {
+                                                uint8_t* __restrict__ occ, int* __restrict__ status,
+                                                uint32_t* __restrict__ replay) {
     extern __shared__ uint2 smem_stack[];
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -103,10 +117,16 @@ __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __res
         while (T.template step<ANY>(bvh, r)) {
         }
     if (T.overflow) atomicMax(status, 6);
-    if (ANY)
+    if (ANY) {
         occ[i] = T.found ? 1 : 0;
-    else
-        hits[i] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+    } else {
+        if (T.nan_hit) {
+            hits[i] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+            *replay = 1u;
+        } else {
+            hits[i] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        }
+    }
 }
 
 // 4-wide traversal with persistent warps refilling idle lanes (see
@@ -117,9 +137,11 @@ __global__ void __launch_bounds__(128) k_trace4(DevBVH4 bvh, const float4* __res
 // and no warp is left with a long tail.
 template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
 __global__ void __launch_bounds__(128, MINB)
-    k_trace4_persistent(DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n, const uint32_t* __restrict__ order,
+    k_trace4_persistent(const __grid_constant__ DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
+                        const uint32_t* __restrict__ order,
                         float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status,
-                        uint32_t per_warp, uint32_t refill, uint32_t* __restrict__ work) {
+                        uint32_t per_warp, uint32_t refill, uint32_t* __restrict__ work,
+                        uint32_t* __restrict__ replay) {
     extern __shared__ uint2 smem_stack[];
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -172,10 +194,16 @@ __global__ void __launch_bounds__(128, MINB)
         }
         if (busy && !T.template step<ANY>(bvh, r)) {
             overflow |= T.overflow;
-            if (ANY)
+            if (ANY) {
                 occ[ray] = T.found ? 1 : 0;
-            else
-                hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+            } else {
+                if (T.nan_hit) {
+                    hits[ray] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+                    *replay = 1u;
+                } else {
+                    hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+                }
+            }
             ray = kNone;
         }
     }
@@ -324,14 +352,53 @@ static void read_variant() {
     }
     if (const char* v = getenv("PBRT_RENDER_KERNEL")) {
         int k = variant_from_name(v, g_render_kernel);
-        if (k == kVariantPairPlain || k == kVariantWidePlain) g_render_kernel = k;
+        if (k >= kVariantPairPlain && k <= kVariantWideSpeculative) g_render_kernel = k;
+    }
+}
+
+// Rewrites the closest hits marked kReplayMark by the EXACT walk (see
+// Traversal in trace.cuh); returns at once when no ray of the launch was
+// marked, so a launch without NaN-distance hits pays one empty kernel.
+template <int SMAX, int OVF, bool INST>
+__global__ void __launch_bounds__(128) k_replay4(const __grid_constant__ DevBVH4 bvh, const float4* __restrict__ rays,
+                                                 uint32_t n, float4* __restrict__ hits,
+                                                 const uint32_t* __restrict__ replay, int* __restrict__ status) {
+    extern __shared__ uint2 smem_stack[];
+    if (*(const volatile uint32_t*)replay == 0u) return;
+    Traversal4<SMAX, OVF, INST, true, true> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (__float_as_int(hits[i].x) != kReplayMark) continue;
+        DRay r = make_dray(__ldg(rays + 2 * i), __ldg(rays + 2 * i + 1));
+        if (T.start(bvh, r)) {
+            while (T.template step<false>(bvh, r)) {
+            }
+        }
+        if (T.overflow) atomicMax(status, 6);
+        hits[i] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+    }
+}
+
+template <int STACK, bool INST>
+__global__ void __launch_bounds__(128) k_replay2(const __grid_constant__ DevBVH bvh, const float4* __restrict__ rays,
+                                                 uint32_t n, float4* __restrict__ hits,
+                                                 const uint32_t* __restrict__ replay, int* __restrict__ status) {
+    if (*(const volatile uint32_t*)replay == 0u) return;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (__float_as_int(hits[i].x) != kReplayMark) continue;
+        DRay r = make_dray(__ldg(rays + 2 * i), __ldg(rays + 2 * i + 1));
+        TraceResult res;
+        int st = 0;
+        traverse<STACK, false, INST, true>(bvh, r, &res, &st);
+        if (st) atomicMax(status, st);
+        hits[i] = make_float4(__int_as_float(res.prim), res.t, res.b1, res.b2);
     }
 }
 
 template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
 static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                           float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
-                                          uint32_t* work) {
+                                          uint32_t* work, uint32_t* replay) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
     static int bps = 0, sms = 0;
@@ -353,14 +420,14 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
         uint64_t w = chunks < warps ? chunks : warps;
         unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
         k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(
-            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work);
+            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work, replay);
         return cudaGetLastError();
     }
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
     k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ,
                                                                                   d_status, per_warp, g_refill,
-                                                                                  nullptr);
+                                                                                  nullptr, replay);
     return cudaGetLastError();
 }
 
@@ -397,27 +464,32 @@ static cudaError_t launch_wide_spec(const DevBVH4& bvh, const float4* r4, uint32
 
 template <int SMAX, int OVF, bool ANY>
 static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order, float4* h4,
-                               uint8_t* occ, int* d_status, cudaStream_t stream, bool persistent, uint32_t* work) {
+                               uint8_t* occ, int* d_status, cudaStream_t stream, bool persistent, uint32_t* work,
+                               uint32_t* replay) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
     if (!persistent) {
         unsigned grid = (unsigned)((n + block - 1) / block);
-        k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status);
+        k_trace4<SMAX, OVF, ANY><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ, d_status, replay);
         return cudaGetLastError();
     }
     if (g_min_blocks == 7)
-        return launch_wide_persistent<SMAX, OVF, ANY, 7>(bvh, r4, n, order, h4, occ, d_status, stream, work);
+        return launch_wide_persistent<SMAX, OVF, ANY, 7>(bvh, r4, n, order, h4, occ, d_status, stream, work,
+                                                         replay);
     if (g_min_blocks == 8)
-        return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, order, h4, occ, d_status, stream, work);
+        return launch_wide_persistent<SMAX, OVF, ANY, 8>(bvh, r4, n, order, h4, occ, d_status, stream, work,
+                                                         replay);
     if (g_min_blocks == 9)
-        return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, order, h4, occ, d_status, stream, work);
-    return launch_wide_persistent<SMAX, OVF, ANY, 0>(bvh, r4, n, order, h4, occ, d_status, stream, work);
+        return launch_wide_persistent<SMAX, OVF, ANY, 9>(bvh, r4, n, order, h4, occ, d_status, stream, work,
+                                                         replay);
+    return launch_wide_persistent<SMAX, OVF, ANY, 0>(bvh, r4, n, order, h4, occ, d_status, stream, work,
+                                                         replay);
 }
 
 int set_trace_config(const PbrtTraceConfig& c) {
     if (c.kernel < kVariantPairPlain || c.kernel > kVariantWideSpeculative || c.refill < 1 || c.refill > 32) return 1;
     if (!(c.min_blocks == 0 || c.min_blocks == 7 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
-    if (c.render_kernel != kVariantPairPlain && c.render_kernel != kVariantWidePlain) return 1;
+    if (c.render_kernel < kVariantPairPlain || c.render_kernel > kVariantWideSpeculative) return 1;
     if (c.reorder > 1) return 1;
     if (!(c.chunk == 0 || (c.chunk >= 32 && c.chunk <= 4096 && c.chunk % 32 == 0))) return 1;
     read_variant();
@@ -459,7 +531,8 @@ int wide_stack_variant(uint32_t bound) {
 
 template <int STACK, bool ANY, bool INST = false>
 static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, const uint32_t* order,
-                                     float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream) {
+                                     float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
+                                     uint32_t* replay) {
     static int blocks_per_sm[2][2] = {{0, 0}, {0, 0}};
     static int sms = 0;
     const int block = 128;
@@ -477,7 +550,7 @@ static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
     k_trace_persistent<STACK, ANY, INST><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, occ, d_status, per_warp,
-                                                                     g_refill);
+                                                                     g_refill, replay);
     return cudaGetLastError();
 }
 
@@ -487,11 +560,10 @@ int trace_stack_for_depth(uint32_t depth) {
     return 0;
 }
 
-cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
-                         uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
-                         uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work) {
-    if (n == 0) return cudaSuccess;
-    read_variant();
+static cudaError_t launch_main(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
+                               uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
+                               uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work,
+                               uint32_t* replay) {
     if (bvh.insts) {
         // a scene with instances: the persistent walk with nested instance
         // traversal (4-wide when a variant covers the stack bound),
@@ -503,20 +575,20 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
         const int v = wide ? wide_stack_variant(wide_bound) : 0;
         if (v == 64)
             return any ? launch_wide_persistent<16, 48, true, 0, true>(*wide, r4, n, order, nullptr, occluded, d_status,
-                                                                       stream, work)
+                                                                       stream, work, replay)
                        : launch_wide_persistent<16, 48, false, 0, true>(*wide, r4, n, order, h4, nullptr, d_status,
-                                                                        stream, work);
+                                                                        stream, work, replay);
         if (v == 256)
             return any ? launch_wide_persistent<16, 240, true, 0, true>(*wide, r4, n, order, nullptr, occluded,
-                                                                        d_status, stream, work)
+                                                                        d_status, stream, work, replay)
                        : launch_wide_persistent<16, 240, false, 0, true>(*wide, r4, n, order, h4, nullptr, d_status,
-                                                                         stream, work);
+                                                                         stream, work, replay);
         if (stack == 64)
-            return any ? launch_persistent<64, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
-                       : launch_persistent<64, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<64, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream, replay)
+                       : launch_persistent<64, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream, replay);
         if (stack == 256)
-            return any ? launch_persistent<256, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
-                       : launch_persistent<256, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<256, true, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream, replay)
+                       : launch_persistent<256, false, true>(bvh, r4, n, order, h4, nullptr, d_status, stream, replay);
         return cudaErrorInvalidValue;
     }
     const int variant = kernel >= 0 ? kernel : g_kernel_variant;
@@ -538,11 +610,11 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
         const bool any = occluded != nullptr, pt = variant == kVariantWidePersistent;
         int v = wide_stack_variant(wide_bound);
         if (v == 64)
-            return any ? launch_wide<16, 48, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work)
-                       : launch_wide<16, 48, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work);
+            return any ? launch_wide<16, 48, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work, replay)
+                       : launch_wide<16, 48, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work, replay);
         if (v == 256)
-            return any ? launch_wide<16, 240, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work)
-                       : launch_wide<16, 240, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work);
+            return any ? launch_wide<16, 240, true>(*wide, r4, n, order, nullptr, occluded, d_status, stream, pt, work, replay)
+                       : launch_wide<16, 240, false>(*wide, r4, n, order, h4, nullptr, d_status, stream, pt, work, replay);
     }
     const int block = 128;
     const unsigned grid = (unsigned)((n + block - 1) / block);
@@ -552,26 +624,64 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     bool any = occluded != nullptr;
     if (variant == kVariantPairPersistent) {
         if (stack == 64)
-            return any ? launch_persistent<64, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
-                       : launch_persistent<64, false>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<64, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream, replay)
+                       : launch_persistent<64, false>(bvh, r4, n, order, h4, nullptr, d_status, stream, replay);
         if (stack == 256)
-            return any ? launch_persistent<256, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream)
-                       : launch_persistent<256, false>(bvh, r4, n, order, h4, nullptr, d_status, stream);
+            return any ? launch_persistent<256, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream, replay)
+                       : launch_persistent<256, false>(bvh, r4, n, order, h4, nullptr, d_status, stream, replay);
         return cudaErrorInvalidValue;
     }
     if (stack == 64) {
         if (any)
-            k_trace<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status);
+            k_trace<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status, replay);
         else
-            k_trace<64, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status);
+            k_trace<64, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status, replay);
     } else if (stack == 256) {
         if (any)
-            k_trace<256, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status);
+            k_trace<256, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status, replay);
         else
-            k_trace<256, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status);
+            k_trace<256, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status, replay);
     } else {
         return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
+                         uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
+                         uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work, uint32_t* replay) {
+    if (n == 0) return cudaSuccess;
+    if (!occluded && !replay) return cudaErrorInvalidValue;
+    read_variant();
+    cudaError_t e = launch_main(bvh, depth, rays, n, hits, occluded, d_status, stream, wide, wide_bound, kernel, order,
+                                work, replay);
+    if (e != cudaSuccess || occluded) return e;
+    // the replay pass of closest hits (one empty launch unless a ray was marked)
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
+    }
+    const unsigned grid = (unsigned)(sms * 4);
+    const float4* r4 = reinterpret_cast<const float4*>(rays);
+    float4* h4 = reinterpret_cast<float4*>(hits);
+    const bool inst = bvh.insts != nullptr;
+    const int v = wide ? wide_stack_variant(wide_bound) : 0;
+    const size_t smem = 16 * sizeof(uint2) * 128;
+    if (v == 64)
+        inst ? k_replay4<16, 48, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status)
+             : k_replay4<16, 48, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status);
+    else if (v == 256)
+        inst ? k_replay4<16, 240, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status)
+             : k_replay4<16, 240, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status);
+    else if (trace_stack_for_depth(depth) == 64)
+        inst ? k_replay2<64, true><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status)
+             : k_replay2<64, false><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status);
+    else
+        inst ? k_replay2<256, true><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status)
+             : k_replay2<256, false><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status);
     return cudaGetLastError();
 }
 

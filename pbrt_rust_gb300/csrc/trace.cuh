@@ -342,12 +342,22 @@ __device__ __forceinline__ bool analytic_test(const SphereRec* spheres, const De
 // (ANY = true, stopping at the first accepted primitive).  INST: the
 // tree may hold instance records; kernels take INST only for scenes that
 // have instances, so the others keep the registers of the plain walk.
-template <int STACK, bool INST = false>
+//
+// Replay: child boxes are decided against the maxt of the moment they are
+// pushed.  The reference decides them when popped; the two agree because
+// maxt only shrinks - except that a primitive test with t = NaN (NaN or
+// infinite geometry, overflowing products) is accepted by the reference,
+// whose later box tests then ignore maxt.  A closest-hit walk that
+// accepted such a hit (nan_hit) is therefore replayed from the root by the
+// kernels with EXACT, where children are pushed on their box alone and maxt
+// is checked when they are taken, as the reference does.
+template <int STACK, bool INST = false, bool EXACT = false>
 struct Traversal {
     float maxt;
     uint32_t a, b;
     int sp;
     bool found;
+    bool nan_hit;  // a NaN-distance hit was accepted: the result needs an EXACT replay
     TraceResult res;
     uint32_t st_a[STACK];
     uint32_t st_b[STACK];
@@ -356,6 +366,7 @@ struct Traversal {
     __device__ __forceinline__ bool start(const DevBVH& bvh, const DRay& r) {
         maxt = r.tmax;
         found = false;
+        nan_hit = false;
         sp = 0;
         res.prim = -1;
         res.t = 0.0f;
@@ -394,6 +405,7 @@ struct Traversal {
                 if (hit) {
                     maxt = t;
                     found = true;
+                    nan_hit |= !(t == t);
                     res.prim = (int32_t)((id & ~kSphereBit) + add);
                     res.t = t;
                     res.b1 = b1;
@@ -407,12 +419,13 @@ struct Traversal {
             float4 c1a = ldg4(&np->c[1].lo_x), c1b = ldg4(&np->c[1].hi_x);
             float t0, t1;
             bool h0, h1;
+            const float lim = EXACT ? __int_as_float(0x7f800000) : maxt;  // replay: box alone
             if (r.neg & kRayClean) {
-                h0 = slab_clean(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
-                h1 = slab_clean(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+                h0 = slab_clean(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, lim, &t0);
+                h1 = slab_clean(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, lim, &t1);
             } else {
-                h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
-                h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+                h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, lim, &t0);
+                h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, lim, &t1);
             }
             // Near child: child1 unless dir_is_neg[axis] (bvh.rs:409-415).
             bool swap = (r.neg >> b) & 1u;
@@ -422,6 +435,11 @@ struct Traversal {
             uint32_t fb = swap ? __float_as_uint(c0b.w) : __float_as_uint(c1b.w);
             bool hn = swap ? h1 : h0, hf = swap ? h0 : h1;
             float tf = swap ? t0 : t1;
+            if (EXACT) {  // a child taken now must also pass maxt now; a pushed one is checked when popped
+                const float tn = swap ? t1 : t0;
+                hn = hn && !(tn > maxt);
+                if (!hn) hf = hf && !(tf > maxt);
+            }
             if (hn) {
                 if (hf) {
                     if (sp == STACK) {
@@ -456,16 +474,23 @@ struct Traversal {
     }
 };
 
-// Whole traversal of one ray.
-template <int STACK, bool ANY, bool INST = false>
-__device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status) {
-    Traversal<STACK, INST> T;
+// Whole traversal of one ray.  `*nan_hit`: the closest hit needs an EXACT
+// replay (see Traversal).
+template <int STACK, bool ANY, bool INST = false, bool EXACT = false>
+__device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, TraceResult* res, int* status,
+                                         bool* nan_hit = nullptr) {
+    Traversal<STACK, INST, EXACT> T;
     if (T.start(bvh, r)) {
         while (T.template step<ANY>(bvh, r, status)) {
         }
     }
     *res = T.res;
+    if (nan_hit) *nan_hit = T.nan_hit;
     return T.found;
 }
+
+// A closest hit whose walk accepted a NaN distance is written with this
+// prim value and rewritten by the replay kernels.
+constexpr int32_t kReplayMark = -2;
 
 }  // namespace pbrt

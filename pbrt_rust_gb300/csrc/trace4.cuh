@@ -123,13 +123,17 @@ struct InstWalk {
 template <>
 struct InstWalk<false> {};
 
-template <int SMAX, int OVF, bool INST = false, bool LD256 = true>
+//
+// EXACT: the replay walk (Traversal in trace.cuh): children are pushed on
+// their box alone and checked against maxt when taken.
+template <int SMAX, int OVF, bool INST = false, bool LD256 = true, bool EXACT = false>
 struct Traversal4 : InstWalk<INST> {
     float maxt;
     uint32_t cur;
     int sp;
     bool found;
     bool overflow;
+    bool nan_hit;  // a NaN-distance hit was accepted: the result needs an EXACT replay
     TraceResult res;
     uint2* sstack;  // this thread's column: entry k at sstack[k * stride]
     uint32_t stride;
@@ -163,6 +167,7 @@ struct Traversal4 : InstWalk<INST> {
         maxt = r.tmax;
         found = false;
         overflow = false;
+        nan_hit = false;
         sp = 0;
         res.prim = -1;
         res.t = 0.0f;
@@ -218,7 +223,8 @@ struct Traversal4 : InstWalk<INST> {
         float o[3], d[3];
         xf_point(S->w2o, r.ox, r.oy, r.oz, o);  // transform.rs:230-237
         xf_vector(S->w2o, r.dx, r.dy, r.dz, d);
-        const DRay ri = make_dray(make_float4(o[0], o[1], o[2], r.tmin), make_float4(d[0], d[1], d[2], maxt));
+        // (tmax is not read while walking; it keeps the world ray's for a replay)
+        const DRay ri = make_dray(make_float4(o[0], o[1], o[2], r.tmin), make_float4(d[0], d[1], d[2], r.tmax));
         const DevBVH4& D = bvh.insts[S->instance];
         float tr;
         const ChildRec& Rt = D.root;
@@ -285,6 +291,7 @@ struct Traversal4 : InstWalk<INST> {
             if (hit) {
                 maxt = t;
                 found = true;
+                nan_hit |= !(t == t);
                 if constexpr (INST)
                     res.prim = (int32_t)(this->base_ + (id & ~kSphereBit));
                 else
@@ -299,6 +306,7 @@ struct Traversal4 : InstWalk<INST> {
         }
     }
 
+    // One unit of work; false once the ray is finished.
     template <bool ANY, class R>
     __device__ __forceinline__ bool step(const DevBVH4& bvh, R& r) {
         if constexpr (INST) {
@@ -335,16 +343,17 @@ struct Traversal4 : InstWalk<INST> {
         }
         float t0, t1, t2, t3;
         bool h0, h1, h2, h3;
+        const float lim = EXACT ? __int_as_float(0x7f800000) : maxt;  // replay: box alone
         if (r.neg & kRayClean) {
-            h0 = c0.a != kNode4Empty && slab_clean(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
-            h1 = c1.a != kNode4Empty && slab_clean(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
-            h2 = c2.a != kNode4Empty && slab_clean(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
-            h3 = c3.a != kNode4Empty && slab_clean(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+            h0 = c0.a != kNode4Empty && slab_clean(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, lim, &t0);
+            h1 = c1.a != kNode4Empty && slab_clean(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, lim, &t1);
+            h2 = c2.a != kNode4Empty && slab_clean(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, lim, &t2);
+            h3 = c3.a != kNode4Empty && slab_clean(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, lim, &t3);
         } else {
-            h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, maxt, &t0);
-            h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, maxt, &t1);
-            h2 = c2.a != kNode4Empty && slab(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, maxt, &t2);
-            h3 = c3.a != kNode4Empty && slab(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, maxt, &t3);
+            h0 = c0.a != kNode4Empty && slab(c0.lx, c0.ly, c0.lz, c0.hx, c0.hy, c0.hz, r, lim, &t0);
+            h1 = c1.a != kNode4Empty && slab(c1.lx, c1.ly, c1.lz, c1.hx, c1.hy, c1.hz, r, lim, &t1);
+            h2 = c2.a != kNode4Empty && slab(c2.lx, c2.ly, c2.lz, c2.hx, c2.hy, c2.hz, r, lim, &t2);
+            h3 = c3.a != kNode4Empty && slab(c3.lx, c3.ly, c3.lz, c3.hx, c3.hy, c3.hz, r, lim, &t3);
         }
         if (!(h0 | h1 | h2 | h3)) return pop();
         const uint32_t meta = c0.b;
@@ -358,6 +367,23 @@ struct Traversal4 : InstWalk<INST> {
         cswap(sR, a2, a3, h2, h3, t2, t3);
         cswap(sN, a0, a2, h0, h2, t0, t2);
         cswap(sN, a1, a3, h1, h3, t1, t3);
+        if (EXACT) {
+            // replay: the reference takes the first child whose box passes
+            // maxt now, culls the ones before it now, and tests the pushed
+            // ones against maxt when it pops them
+            bool scan = true;
+            if (scan && h0) {
+                if (t0 > maxt) h0 = false; else scan = false;
+            }
+            if (scan && h1) {
+                if (t1 > maxt) h1 = false; else scan = false;
+            }
+            if (scan && h2) {
+                if (t2 > maxt) h2 = false; else scan = false;
+            }
+            if (scan && h3 && t3 > maxt) h3 = false;
+            if (!(h0 | h1 | h2 | h3)) return pop();
+        }
         const int first = h0 ? 0 : (h1 ? 1 : (h2 ? 2 : 3));
         if (h3 && first < 3) push(a3, t3);
         if (h2 && first < 2) push(a2, t2);
@@ -384,7 +410,13 @@ __device__ __noinline__ TraceResult instance_test(const DevBVH4* insts, const Sp
         while (T.template step<ANY>(B, ri)) {
         }
     }
-    return T.res;
+    if (ANY || !T.nan_hit) return T.res;
+    Traversal4<0, kInstStack4, false, false, true> E;  // replay
+    if (E.start(B, ri)) {
+        while (E.template step<false>(B, ri)) {
+        }
+    }
+    return E.res;
 }
 
 }  // namespace pbrt

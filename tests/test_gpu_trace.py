@@ -292,3 +292,78 @@ def test_disks_and_cylinders_match_oracle(oracle, kernel):
     g2, o2 = GpuBVHAccel(full_only, 4, "sah"), oracle.OracleBVH(full_only, 4, "sah")
     assert np.array_equal(g2.intersect(rays).view(np.uint32), o2.intersect(rays).view(np.uint32))
     assert np.array_equal(g2.intersect_p(rays), o2.intersect_p(rays))
+
+
+def degenerate_scene_and_rays(n_tris: int = 600, seed: int = 5, nonfinite: bool = False):
+    """Triangles with vertices on a 0.25 grid (rays can run exactly along box
+    planes and through corners) - with `nonfinite`, some with NaN or infinite
+    coordinates - and rays that start on grid planes with directions that
+    have +-0, denormal, tiny or large components (with `nonfinite`, so large
+    that the triangle test overflows), plus reversed [tmin, tmax] and
+    infinite tmax."""
+    rng = np.random.default_rng(seed)
+    pts = (rng.integers(-8, 9, size=(n_tris, 3, 3)) * 0.25).astype(np.float32)
+    if nonfinite:
+        pts[5, 0, 0] = np.nan
+        pts[6, :, 1] = np.nan
+        pts[7, 1, 2] = np.inf
+        pts[8, :, :] = np.nan
+        pts[9, 2, 0] = -np.inf
+    mesh = Shape.triangle_mesh(Transform(), None, False, np.arange(3 * n_tris, dtype=np.uint32), pts.reshape(-1, 3))
+    n = 1 << 14
+    r = np.zeros(n, dtype=abi.RAY_DTYPE)
+    r["o"] = (rng.integers(-12, 13, size=(n, 3)) * 0.25).astype(np.float32)
+    d = rng.integers(-2, 3, size=(n, 3)).astype(np.float32)
+    d[d.sum(axis=1) == 0, 0] = 1.0
+    huge = 3.0e38 if nonfinite else 1.0e30  # 3e38 overflows the triangle test's products to NaN
+    special = np.array([0.0, -0.0, 1e-40, -1e-40, 1e-30, huge], np.float32)
+    k = np.arange(n) % 3 == 0
+    d[k, rng.integers(0, 3, size=n)[k]] = special[rng.integers(0, 6, size=n)[k]]
+    r["d"] = d
+    r["tmin"] = np.where(np.arange(n) % 17 == 0, 5.0, 0.0).astype(np.float32)
+    r["tmax"] = np.where(np.arange(n) % 5 == 0, np.inf, np.where(np.arange(n) % 17 == 0, 1.0, 8.0)).astype(np.float32)
+    return mesh, r
+
+
+def same_hits(a, b):
+    """Equal hits, a NaN equal to any NaN (device and host NaN payloads differ)."""
+    if not np.array_equal(a["prim"], b["prim"]):
+        return False
+    return all(np.array_equal(a[f], b[f], equal_nan=True) for f in ("t", "b1", "b2"))
+
+
+def test_degenerate_rays_match_oracle(oracle, kernel):
+    """Both slab tests (the min/max one for rays with finite origin and 1/d,
+    the literal one for the others) against the oracle on grid-aligned
+    geometry.  A direction with a tiny component can overflow the triangle
+    test's 1/divisor, giving a hit with NaN barycentrics as in the
+    reference; NaN payloads differ between device and host."""
+    mesh, rays = degenerate_scene_and_rays()
+    for mp in (1, 4):
+        g, o = GpuBVHAccel([mesh], mp, "sah"), oracle.OracleBVH([mesh], mp, "sah")
+        want = o.intersect(rays)
+        assert (want["prim"] >= 0).sum() > 2000
+        assert same_hits(dev_hits(g, rays), want)
+        assert np.array_equal(dev_any(g, rays), o.intersect_p(rays))
+
+
+@pytest.mark.parametrize("name", ["plain", "pt", "w4", "w4pt"])
+def test_nonfinite_vertices_match_oracle(oracle, name):
+    """Triangles with NaN or infinite vertices and overflowing directions: a
+    triangle test can accept a hit with t or barycentrics NaN (comparisons
+    with NaN are false), as the reference does, after which the reference's
+    box tests ignore maxt; walks that accepted a NaN distance are replayed
+    in exact mode.  Equal to the oracle (NaN payloads aside).  The
+    speculative-leaf kernel assumes hits lie inside their boxes and is left
+    out."""
+    before = abi.get_trace_config()
+    abi.set_trace_config(kernel=name)
+    try:
+        mesh, rays = degenerate_scene_and_rays(nonfinite=True)
+        g, o = GpuBVHAccel([mesh], 1, "sah"), oracle.OracleBVH([mesh], 1, "sah")
+        want = o.intersect(rays)
+        assert np.isnan(want["t"]).sum() > 50
+        assert same_hits(dev_hits(g, rays), want)
+        assert np.array_equal(dev_any(g, rays), o.intersect_p(rays))
+    finally:
+        abi.set_trace_config(**before)
