@@ -380,7 +380,10 @@ typedef struct PbrtBatchLimits {
     uint64_t max_query_rays;    /* rays of query jobs with host buffers */
 } PbrtBatchLimits;
 
-/* Launch choices of a batch (the autotuner's search space). */
+/* Launch choices of a batch (the autotuner's search space).  A new batch
+ * starts with 4-wide extend and shadow walks (binary where a job's tree has
+ * no 4-wide layout), 128 threads, 16 stack entries, chunk 64, refill 32 /
+ * 32, graphs on. */
 typedef struct PbrtBatchTuning {
     int32_t extend_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and query rays */
     int32_t shadow_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: shadow rays */

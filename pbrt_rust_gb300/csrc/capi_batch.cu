@@ -115,7 +115,7 @@ struct PbrtBatch {
     std::vector<Copy> h2d, d2h;  // staged host inputs / outputs of the jobs
     bool in_flight = false;
 
-    BatchTuning tune{0, 0, 128, 16, 64, 32, 32};
+    BatchTuning tune{1, 1, 128, 16, 64, 32, 32};  // 4-wide walks where every job has the layout
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
     BatchTuning graph_tune{};

@@ -27,7 +27,7 @@ class GpuServer:
         if tuning:
             cfg.use_tuning = 1
             t = abi.PbrtBatchTuning()
-            base = dict(extend_kernel="pair", shadow_kernel="pair", block=128, stack=16, chunk=64, refill=32,
+            base = dict(extend_kernel="wide", shadow_kernel="wide", block=128, stack=16, chunk=64, refill=32,
                         refill_shadow=32, use_graph=1)
             base.update(tuning)
             for k, v in base.items():
