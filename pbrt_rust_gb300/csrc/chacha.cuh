@@ -64,35 +64,37 @@ __device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr
 }
 #undef PBRT_QR
 
-// A seekable reader of one task's word stream.
+// A seekable reader of one task's word stream.  Blocks are computed when a
+// word of them is read, so words skipped over (whole blocks of them) cost
+// nothing.
 struct WordStream {
     uint32_t key[8];
-    uint64_t block;
+    uint64_t block;   // block of the next word
+    uint64_t loaded;  // block held in buf (~0: none)
     uint32_t buf[16];
-    int idx;
+    int idx;          // next word inside `block` (16: the block is used up)
 
     __device__ void seek(const uint32_t* k, uint64_t word) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) key[i] = k[i];
         block = word >> 4;
         idx = (int)(word & 15);
-        chacha12_block(key, block, buf);
+        loaded = ~0ull;
     }
     // Moves n words ahead without reading them.
     __device__ __forceinline__ void skip(uint32_t n) {
         const uint64_t pos = block * 16u + (uint64_t)idx + n;
-        const uint64_t nb = pos >> 4;
+        block = pos >> 4;
         idx = (int)(pos & 15u);
-        if (nb != block) {
-            block = nb;
-            chacha12_block(key, block, buf);
-        }
     }
     __device__ __forceinline__ uint32_t next_u32() {
         if (idx == 16) {
             ++block;
-            chacha12_block(key, block, buf);
             idx = 0;
+        }
+        if (block != loaded) {
+            chacha12_block(key, block, buf);
+            loaded = block;
         }
         return buf[idx++];
     }
