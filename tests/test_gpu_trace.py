@@ -367,3 +367,23 @@ def test_nonfinite_vertices_match_oracle(oracle, name):
         assert np.array_equal(dev_any(g, rays), o.intersect_p(rays))
     finally:
         abi.set_trace_config(**before)
+
+
+def test_pipelined_host_buffers_equal_device_buffers():
+    """Host-buffer calls of 2^19+ rays run in chunks whose copies overlap
+    the other chunks' traversal; every hit must land as with device
+    buffers, for pageable and pinned host memory and a ray count that does
+    not divide into the chunks."""
+    torch = _torch()
+    prims, _ = G.ray_soup(4096, 1, seed=4)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    rays = G.incoherent_rays(G.PCG32(31), (1 << 20) + 12345, lo, hi)
+    want, want_any = dev_hits(g, rays), dev_any(g, rays)
+    assert (want["prim"] >= 0).sum() > 10000
+    assert np.array_equal(g.intersect(rays).view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(g.intersect_p(rays), want_any)
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    out = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory()
+    g.intersect(pinned, out=out)
+    assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
