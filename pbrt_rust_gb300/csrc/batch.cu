@@ -49,12 +49,13 @@ __device__ __forceinline__ uint32_t locate(const uint64_t* __restrict__ off, uin
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_generate(BatchArgs A) {
+    __shared__ uint32_t words[16 * BLOCK];  // the threads' ChaCha blocks
     const uint64_t total = A.hdr->pix;
     const uint32_t nj = A.hdr->n_jobs;
     Cursor c{0, 1, 0};
     for (uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; g < total; g += (uint64_t)gridDim.x * BLOCK) {
         const uint32_t j = locate(A.off_pix, nj, g, c);
-        generate_pixel(A.jobs[j].P, (uint32_t)(g - c.lo));
+        generate_pixel(A.jobs[j].P, (uint32_t)(g - c.lo), words + threadIdx.x, (uint32_t)BLOCK);
     }
 }
 

@@ -29,7 +29,8 @@ __device__ __forceinline__ uint32_t rotl32(uint32_t v, int c) { return __funnels
     b ^= c;                 \
     b = rotl32(b, 7);
 
-__device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr, uint32_t out[16]) {
+// out[k * stride] = keystream word k of block `ctr`.
+__device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride) {
     uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
     uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
     uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
@@ -45,41 +46,46 @@ __device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr
         PBRT_QR(x2, x7, x8, x13);
         PBRT_QR(x3, x4, x9, x14);
     }
-    out[0] = x0 + 0x61707865u;
-    out[1] = x1 + 0x3320646eu;
-    out[2] = x2 + 0x79622d32u;
-    out[3] = x3 + 0x6b206574u;
-    out[4] = x4 + key[0];
-    out[5] = x5 + key[1];
-    out[6] = x6 + key[2];
-    out[7] = x7 + key[3];
-    out[8] = x8 + key[4];
-    out[9] = x9 + key[5];
-    out[10] = x10 + key[6];
-    out[11] = x11 + key[7];
-    out[12] = x12 + (uint32_t)ctr;
-    out[13] = x13 + (uint32_t)(ctr >> 32);
-    out[14] = x14;
-    out[15] = x15;
+    out[0u * stride] = x0 + 0x61707865u;
+    out[1u * stride] = x1 + 0x3320646eu;
+    out[2u * stride] = x2 + 0x79622d32u;
+    out[3u * stride] = x3 + 0x6b206574u;
+    out[4u * stride] = x4 + key[0];
+    out[5u * stride] = x5 + key[1];
+    out[6u * stride] = x6 + key[2];
+    out[7u * stride] = x7 + key[3];
+    out[8u * stride] = x8 + key[4];
+    out[9u * stride] = x9 + key[5];
+    out[10u * stride] = x10 + key[6];
+    out[11u * stride] = x11 + key[7];
+    out[12u * stride] = x12 + (uint32_t)ctr;
+    out[13u * stride] = x13 + (uint32_t)(ctr >> 32);
+    out[14u * stride] = x14;
+    out[15u * stride] = x15;
 }
 #undef PBRT_QR
 
 // A seekable reader of one task's word stream.  Blocks are computed when a
 // word of them is read, so words skipped over (whole blocks of them) cost
-// nothing.
+// nothing.  The current block lives in the caller's shared-memory column
+// (word k at buf[k * stride]): a per-thread array would go to local memory,
+// whose loads and stores throttle the generate kernels.
 struct WordStream {
     uint32_t key[8];
     uint64_t block;   // block of the next word
     uint64_t loaded;  // block held in buf (~0: none)
-    uint32_t buf[16];
+    uint32_t* buf;
+    uint32_t stride;
     int idx;          // next word inside `block` (16: the block is used up)
 
-    __device__ void seek(const uint32_t* k, uint64_t word) {
+    __device__ void seek(const uint32_t* k, uint64_t word, uint32_t* column, uint32_t column_stride) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) key[i] = k[i];
         block = word >> 4;
         idx = (int)(word & 15);
         loaded = ~0ull;
+        buf = column;
+        stride = column_stride;
     }
     // Moves n words ahead without reading them.
     __device__ __forceinline__ void skip(uint32_t n) {
@@ -93,10 +99,10 @@ struct WordStream {
             idx = 0;
         }
         if (block != loaded) {
-            chacha12_block(key, block, buf);
+            chacha12_block(key, block, buf, stride);
             loaded = block;
         }
-        return buf[idx++];
+        return buf[(uint32_t)idx++ * stride];
     }
     __device__ __forceinline__ uint64_t next_u64() {  // low word first
         uint64_t lo = next_u32();

@@ -105,8 +105,10 @@ __device__ __forceinline__ void camera_ray(const RenderParams& P, const float* r
     out->tmax = FLT_MAX;  // ray.rs:36
 }
 
-// One sampler pixel (k_generate's item).
-__device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t pix) {
+// One sampler pixel (k_generate's item).  `rng_col`: this thread's column
+// of 16 words in shared memory (word k at rng_col[k * stride]).
+__device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t pix, uint32_t* rng_col,
+                                               uint32_t stride) {
     int32_t sw = P.sx1 - P.sx0;
     int32_t x = P.sx0 + (int32_t)(pix % (uint32_t)sw);
     int32_t y = P.sy0 + (int32_t)(pix / (uint32_t)sw);
@@ -129,7 +131,7 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
     const TaskRec& T = P.tasks[t];
     uint64_t j = (uint64_t)(y - T.wy0) * (uint64_t)(T.wx1 - T.wx0) + (uint64_t)(x - T.wx0);
     WordStream rng;
-    rng.seek(T.key, j * P.words_per_pixel);
+    rng.seek(T.key, j * P.words_per_pixel, rng_col, stride);
     const bool jit = P.jitter != 0;
     if (!(P.lens_radius > 0.0f)) {
         // Pinhole camera: the ray depends on the image position alone, so
