@@ -117,7 +117,7 @@ struct InstWalk {
     const Node4* nodes_;
     const PrimRec* prims_;
     const SphereRec* spheres_;
-    float wox_, woy_, woz_, wdx_, wdy_, wdz_;
+    DRay world_;  // the world ray while inside an instance
     uint32_t base_;
 };
 template <>
@@ -231,12 +231,7 @@ struct Traversal4 : InstWalk<INST> {
         if (D.empty || !slab(Rt.lo_x, Rt.lo_y, Rt.lo_z, Rt.hi_x, Rt.hi_y, Rt.hi_z, ri, maxt, &tr)) return false;
         if (resume) push(resume, __int_as_float(0xff800000));  // -inf: always taken
         push(kExitInst, __int_as_float(0xff800000));
-        this->wox_ = r.ox;
-        this->woy_ = r.oy;
-        this->woz_ = r.oz;
-        this->wdx_ = r.dx;
-        this->wdy_ = r.dy;
-        this->wdz_ = r.dz;
+        this->world_ = r;
         r = ri;
         this->nodes_ = D.nodes;
         this->prims_ = D.prims;
@@ -246,12 +241,10 @@ struct Traversal4 : InstWalk<INST> {
         return !overflow;
     }
 
-    // INST: back to the scene's tree and the world ray (make_dray gives the
-    // same 1/d and signs as at the start).
+    // INST: back to the scene's tree and the world ray.
     template <class R>
     __device__ __forceinline__ void leave(const DevBVH4& bvh, R& r) {
-        r = make_dray(make_float4(this->wox_, this->woy_, this->woz_, r.tmin),
-                      make_float4(this->wdx_, this->wdy_, this->wdz_, r.tmax));
+        r = this->world_;
         this->nodes_ = bvh.nodes;
         this->prims_ = bvh.prims;
         this->spheres_ = bvh.spheres;
