@@ -229,17 +229,17 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
 
 // Host-buffer calls of at least 2 * kPipeChunkMin rays run in
 // pipe_chunks() chunks (PBRT_PIPE_CHUNKS: 1 = one piece, at most
-// kPipeChunks; default 3) whose copies overlap the other chunks' traversal.
-// Measured on GB300 with 2^22 heightfield rays and pinned buffers: 2.32 ms
-// in one piece, 1.82 ms in 3 chunks, 1.87 / 1.93 / 2.04 / 2.30 ms in 4 / 5
-// / 6 / 8 (each chunk adds launches and a kernel tail; the copies' traffic
-// also evicts BVH lines from L2).
+// kPipeChunks; default 4) whose copies overlap the other chunks' traversal;
+// consecutive chunks trace on two streams so that one kernel's tail overlaps
+// the next one's start.  Measured on GB300 with 2^22 heightfield rays and
+// pinned buffers: 2.32 ms in one piece; 1.84 / 1.76 / 1.77 ms in 3 / 4 / 6
+// chunks (one compute stream: 1.82 / 1.87 / 2.04 ms).
 constexpr uint32_t kPipeChunkMin = 1u << 18;
 constexpr uint32_t kPipeChunks = 8;
 static uint32_t pipe_chunks() {
     static const uint32_t k = [] {
         const char* v = getenv("PBRT_PIPE_CHUNKS");
-        const int x = v ? atoi(v) : 3;
+        const int x = v ? atoi(v) : 4;
         return (uint32_t)(x < 1 ? 1 : (x > (int)kPipeChunks ? (int)kPipeChunks : x));
     }();
     return k;
@@ -251,7 +251,8 @@ static int pipe_streams(PbrtBVH* b) {
     if (b->pipe_in) return PBRT_OK;
     int st;
     if ((st = cuda_status(cudaStreamCreateWithFlags(&b->pipe_in, cudaStreamNonBlocking), "cudaStreamCreate")) ||
-        (st = cuda_status(cudaStreamCreateWithFlags(&b->pipe_out, cudaStreamNonBlocking), "cudaStreamCreate")))
+        (st = cuda_status(cudaStreamCreateWithFlags(&b->pipe_out, cudaStreamNonBlocking), "cudaStreamCreate")) ||
+        (st = cuda_status(cudaStreamCreateWithFlags(&b->pipe_k, cudaStreamNonBlocking), "cudaStreamCreate")))
         return st;
     for (cudaEvent_t& e : b->pipe_ev)
         if ((st = cuda_status(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate"))) return st;
@@ -287,8 +288,9 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
     const size_t out_unit = hits ? sizeof(PbrtHit) : 1;
     if (n >= 2 * kPipeChunkMin && pipe_chunks() > 1) {
         // Pipelined: chunk c's copy in (stream pipe_in), traversal (the
-        // caller's stream) and copy out (pipe_out) overlap with the other
-        // chunks' - the copies hide behind the kernels.
+        // caller's stream for even c, pipe_k for odd c) and copy out
+        // (pipe_out) overlap with the other chunks' - the copies hide
+        // behind the kernels.
         if ((st = pipe_streams(b))) return st;
         // the first and last chunks are half the others: the copy before
         // the first traversal and the one after the last are what no
@@ -315,13 +317,14 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
                                       "cudaMemcpyAsync H2D")))
                     return st;
             }
+            cudaStream_t ks = (c & 1) ? b->pipe_k : s;  // alternate compute streams: kernel tails overlap
             if ((st = cuda_status(cudaEventRecord(in_done, b->pipe_in), "cudaEventRecord")) ||
-                (st = cuda_status(cudaStreamWaitEvent(s, in_done, 0), "cudaStreamWaitEvent")))
+                (st = cuda_status(cudaStreamWaitEvent(ks, in_done, 0), "cudaStreamWaitEvent")))
                 return st;
             uint8_t* o = static_cast<uint8_t*>(d_out) + (size_t)lo * out_unit;
-            if ((st = launch_batch(b, d_rays + lo, cnt, hits ? (PbrtHit*)o : nullptr, hits ? nullptr : o, s)))
+            if ((st = launch_batch(b, d_rays + lo, cnt, hits ? (PbrtHit*)o : nullptr, hits ? nullptr : o, ks)))
                 return st;
-            if ((st = cuda_status(cudaEventRecord(traced, s), "cudaEventRecord")) ||
+            if ((st = cuda_status(cudaEventRecord(traced, ks), "cudaEventRecord")) ||
                 (st = cuda_status(cudaStreamWaitEvent(b->pipe_out, traced, 0), "cudaStreamWaitEvent")))
                 return st;
             if (!dout && (st = cuda_status(cudaMemcpyAsync(static_cast<uint8_t*>(out) + (size_t)lo * out_unit, o,
@@ -330,6 +333,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
                 return st;
         }
         if ((st = cuda_status(cudaStreamSynchronize(b->pipe_out), "cudaStreamSynchronize")) ||
+            (st = cuda_status(cudaStreamSynchronize(b->pipe_k), "cudaStreamSynchronize")) ||
             (st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize")))
             return st;
     } else {
@@ -361,6 +365,7 @@ PbrtBVH::~PbrtBVH() {
         if (e) cudaEventDestroy(e);
     if (pipe_in) cudaStreamDestroy(pipe_in);
     if (pipe_out) cudaStreamDestroy(pipe_out);
+    if (pipe_k) cudaStreamDestroy(pipe_k);
     for (void* p : d_inst_bufs) cudaFree(p);
     if (d_insts) cudaFree(d_insts);
     if (d_pairs) cudaFree(d_pairs);

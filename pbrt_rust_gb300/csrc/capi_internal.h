@@ -54,7 +54,7 @@ struct PbrtBVH {
     std::mutex upload_mu;
     std::atomic<bool> uploaded{false};  // device copy made by the first call that needs it
     pbrt::DeviceBuf stage_in, stage_out;
-    cudaStream_t pipe_in = nullptr, pipe_out = nullptr;  // pipelined host-buffer calls
+    cudaStream_t pipe_in = nullptr, pipe_out = nullptr, pipe_k = nullptr;  // pipelined host-buffer calls
     cudaEvent_t pipe_ev[17] = {};                        // entry + 2 per chunk (8 chunks)
     ~PbrtBVH();
 };
