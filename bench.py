@@ -538,7 +538,8 @@ def run_ours(args):
                              "sample": f"{cpu_passes} passes over the 2^22 rays, {cpu_dt:.1f} s"},
             "e2e": {"value": e2e_mrays, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
                     "d2h_bytes_per_step": N_RAYS * 16},
-            "gpu_launches": args.steps,
+            # per timed step: the traversal kernel and the replay check (D24)
+            "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),
             "any_hit": {"value": N_RAYS / (statistics.mean(ms_any) / 1e3) / 1e6, "unit": "Mrays/s"},
             "render_1024x1024_16spp": {"ms_mean": 1e3 * statistics.mean(rt), "ms_min": 1e3 * min(rt),
