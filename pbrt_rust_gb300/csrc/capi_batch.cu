@@ -382,7 +382,7 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
                                           "samples, film pixels or tasks");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(P.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
-    const bool inst = P.bvh.insts != nullptr;  // instances: binary layout only
+    const bool inst = P.bvh.insts != nullptr;  // batches walk instanced jobs over the binary layout
     const uint32_t cw = (P.has_wide && !inst) ? (uint32_t)wide_stack_variant(P.wide_bound) : 0u;
     const uint32_t j = b->n_jobs;
     const Layout& Y = b->lay;
@@ -451,7 +451,7 @@ int pbrtgpu_batch_add_query(PbrtBatch* b, const PbrtBVH* cb, const PbrtRay* rays
         return set_error(PBRT_ERR_BUDGET, "the query does not fit the batch's remaining jobs or staged rays");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(B->host.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
-    const bool inst = B->dev.insts != nullptr;  // instances: binary layout only
+    const bool inst = B->dev.insts != nullptr;  // batches walk instanced jobs over the binary layout
     const DevBVH4* w = inst ? nullptr : wide_of(B);
     const uint32_t cw = w ? (uint32_t)wide_stack_variant(B->host.stack4_bound) : 0u;
     const uint32_t j = b->n_jobs;
