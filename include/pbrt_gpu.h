@@ -109,10 +109,11 @@ typedef struct PbrtShapeDesc {
     int32_t area_light;           /* index into PbrtSceneDesc.lights or -1 */
 } PbrtShapeDesc;
 
-/* Matte material (src/material/matte.rs:30-51) with constant textures. */
+/* Matte material (src/material/matte.rs:30-51) with constant textures:
+ * Lambertian (src/bsdf/lambertian.rs) or Oren-Nayar (src/bsdf/orennayar.rs). */
 typedef struct PbrtMaterialDesc {
     float kd[3];
-    float sigma;                  /* only 0 (Lambertian) is supported */
+    float sigma;                  /* degrees, clamped to [0, 90]: 0 = Lambertian, else Oren-Nayar */
 } PbrtMaterialDesc;
 
 enum { PBRT_LIGHT_POINT = 0, PBRT_LIGHT_DIFFUSE_AREA = 1 };

@@ -1601,9 +1601,29 @@ struct Light {
     float I[3];
     int area;  // index into area lights
 };
+// MatteMaterial::get_bsdf (matte.rs:30-51): Kd clamped to [0, f32::MAX],
+// sigma to [0, 90]; sigma == 0 -> Lambertian, else OrenNayar::new
+// (orennayar.rs:15-28) with its A and B.
+struct Matte {
+    float kd[3];
+    bool oren;
+    float a, b;
+};
+Matte matte_new(const PbrtMaterialDesc& m) {
+    Matte r;
+    for (int c = 0; c < 3; ++c) r.kd[c] = clampf(m.kd[c], 0.0f, FLT_MAX);
+    const float sig = clampf(m.sigma, 0.0f, 90.0f);
+    r.oren = !(sig == 0.0f);
+    const float sigma = sig * kPi / 180.0f;  // utils/mod.rs:37-39
+    const float sigma2 = sigma * sigma;
+    r.a = 1.0f - (sigma2 / (2.0f * (sigma + 0.33f)));
+    r.b = 0.45f * sigma2 / (sigma2 + 0.09f);
+    return r;
+}
+
 struct SceneData {
     OracleBVH bvh;
-    std::vector<PbrtMaterialDesc> materials;
+    std::vector<Matte> materials;
     std::vector<Light> lights;
     std::vector<AreaLight> areas;
 };
@@ -1612,7 +1632,7 @@ int scene_build(const PbrtSceneDesc* d, SceneData* S) {
     SplitMethod sm = (SplitMethod)d->split_method;
     int st = build_aggregate(d->shapes, d->n_shapes, d->instances, d->n_instances, d->max_prims_in_node, sm, &S->bvh);
     if (st) return st;
-    S->materials.assign(d->materials, d->materials + d->n_materials);
+    for (uint32_t i = 0; i < d->n_materials; ++i) S->materials.push_back(matte_new(d->materials[i]));
     for (uint32_t i = 0; i < d->n_lights; ++i) {
         const PbrtLightDesc& L = d->lights[i];
         Light l{};
@@ -1644,17 +1664,17 @@ int scene_build(const PbrtSceneDesc* d, SceneData* S) {
 
 // Surface hit record used by shading.
 struct SurfHit {
-    V3 p, nn;
+    V3 p, nn, dpdu;
     float eps;
     int prim;
     int material, area_light;
 };
 
-// dg.p and dg.nn of refined primitive p (a triangle or a quadric of R) hit
-// by ray r at t.
-void surface_dg(const Refined& R, const Prim& p, const Ray& r, float t, V3* pos, V3* nn) {
+// dg.p, dg.nn and dg.dpdu (world space) of refined primitive p (a triangle
+// or a quadric of R) hit by ray r at t.
+void surface_dg(const Refined& R, const Prim& p, const Ray& r, float t, V3* pos, V3* nn, V3* dpdu) {
     if (p.kind == KIND_TRI) {
-        tri_dg(p.tri, r, t, pos, nn, nullptr);
+        tri_dg(p.tri, r, t, pos, nn, dpdu);
         return;
     }
     const Sphere& s = R.spheres[p.sphere];
@@ -1662,9 +1682,9 @@ void surface_dg(const Refined& R, const Prim& p, const Ray& r, float t, V3* pos,
     float th, phi;
     quad_hit_obj(s, orr, &th, &phi);  // recompute phi for u (same t)
     if (s.kind == QUAD_SPHERE)
-        sphere_dg(s, orr, t, phi, pos, nn, nullptr, nullptr, nullptr, nullptr, nullptr);
+        sphere_dg(s, orr, t, phi, pos, nn, dpdu, nullptr, nullptr, nullptr, nullptr);
     else
-        quad_dg(s, orr, t, phi, pos, nn, nullptr, nullptr, nullptr, nullptr);
+        quad_dg(s, orr, t, phi, pos, nn, nullptr, nullptr, dpdu, nullptr);
 }
 
 bool scene_intersect(const SceneData& S, const Ray& r_in, SurfHit* sh, Counters& C, std::vector<uint32_t>& todo) {
@@ -1683,14 +1703,15 @@ bool scene_intersect(const SceneData& S, const Ray& r_in, SurfHit* sh, Counters&
         const Inst& I = R.insts[p.sphere];
         const Refined& D = R.defs[I.def]->R;
         const Prim& q = D.prims[(uint32_t)h.prim - R.first_id[compact]];
-        V3 pos, nn;
-        surface_dg(D, q, xf_ray(I.w2i, r_in), h.t, &pos, &nn);
+        V3 pos, nn, dpdu;
+        surface_dg(D, q, xf_ray(I.w2i, r_in), h.t, &pos, &nn, &dpdu);
         sh->p = xf_point(I.i2w, pos);
         sh->nn = normalize(xf_normal(I.w2i, nn));
+        sh->dpdu = xf_vector(I.i2w, dpdu);
         sh->material = q.material;
         sh->area_light = -1;
     } else {
-        surface_dg(R, p, r_in, h.t, &sh->p, &sh->nn);
+        surface_dg(R, p, r_in, h.t, &sh->p, &sh->nn, &sh->dpdu);
         sh->material = p.material;
         sh->area_light = p.area_light;
     }
@@ -1763,6 +1784,34 @@ bool sample_light(const SceneData& S, const Light& l, V3 p, float eps, const Lig
     return true;
 }
 
+// OrenNayar::f (orennayar.rs:31-62) without the reflectance: a + b *
+// maxcos * sin(alpha) * tan(beta), with bsdf/utils.rs:5-28.
+inline float sin_theta_l(V3 v) { return sqrtf(fmaxf(0.0f, 1.0f - v.z * v.z)); }
+inline float clamp_unit(float x) { return x < -1.0f ? -1.0f : (x > 1.0f ? 1.0f : x); }
+inline float cos_phi_l(V3 v) {
+    const float st = sin_theta_l(v);
+    return st == 0.0f ? 1.0f : clamp_unit(v.x / st);
+}
+inline float sin_phi_l(V3 v) {
+    const float st = sin_theta_l(v);
+    return st == 0.0f ? 0.0f : clamp_unit(v.y / st);
+}
+float oren_nayar_term(float a, float b, V3 wo, V3 wi) {
+    const float sinthetai = sin_theta_l(wi), sinthetao = sin_theta_l(wo);
+    float maxcos = 0.0f;
+    if (!(sinthetai < 1e-4f || sinthetao < 1e-4f))
+        maxcos = fmaxf(cos_phi_l(wi) * cos_phi_l(wo) + sin_phi_l(wi) * sin_phi_l(wo), 0.0f);
+    float sinalpha, tanbeta;
+    if (fabsf(wi.z) > fabsf(wo.z)) {
+        sinalpha = sinthetao;
+        tanbeta = sinthetai / fabsf(wi.z);
+    } else {
+        sinalpha = sinthetai;
+        tanbeta = sinthetao / fabsf(wo.z);
+    }
+    return a + b * maxcos * sinalpha * tanbeta;
+}
+
 // WhittedIntegrator::li light loop (integrator/whitted.rs:30-65) as the
 // direct-lighting Li (D1), with Lambertian f = Kd/pi when wi, wo lie on the
 // same side of ng (bsdf/mod.rs:132-149, D7), no media (D2).
@@ -1782,9 +1831,13 @@ void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, f
             L[2] = a.L[2];
         }
     }
-    const PbrtMaterialDesc& m = S.materials[h.material];
-    float kd[3] = {clampf(m.kd[0], 0.0f, FLT_MAX), clampf(m.kd[1], 0.0f, FLT_MAX), clampf(m.kd[2], 0.0f, FLT_MAX)};
+    const Matte& m = S.materials[h.material];
+    const float* kd = m.kd;
     float invpi = 1.0f / kPi;  // lambertian.rs:21
+    // BSDF frame (bsdf/mod.rs:70-86): tn = normalize(dpdu), sn = nn x tn,
+    // world_to_local(v) = (v.sn, v.tn, v.nn)
+    V3 tn = normalize(h.dpdu), sn = cross(h.nn, tn);
+    V3 wo_l = mk(dot(wo, sn), dot(wo, tn), dot(wo, h.nn));
     size_t nl = S.lights.size();
     for (size_t li = 0; li < nl; ++li) {
         LightSample ls{light_samples[li], light_samples[nl + 2 * li], light_samples[nl + 2 * li + 1]};
@@ -1796,10 +1849,15 @@ void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, f
         if (black || pdf == 0.0f) continue;
         bool refl = dot(wi, h.nn) * dot(wo, h.nn) > 0.0f;
         float f[3] = {0, 0, 0};
-        if (refl) {
+        if (refl && !m.oren) {
             f[0] = kd[0] * invpi;
             f[1] = kd[1] * invpi;
             f[2] = kd[2] * invpi;
+        } else if (refl) {
+            const float g = oren_nayar_term(m.a, m.b, wo_l, mk(dot(wi, sn), dot(wi, tn), dot(wi, h.nn)));
+            f[0] = kd[0] * invpi * g;
+            f[1] = kd[1] * invpi * g;
+            f[2] = kd[2] * invpi * g;
         }
         if (f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f) continue;
         if (n_shadow) (*n_shadow)++;

@@ -233,9 +233,6 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
                                  "shape " + std::to_string(i) + ": area light must be a diffuse area light on it");
         }
     }
-    for (uint32_t i = 0; i < d->n_materials; ++i)
-        if (d->materials[i].sigma != 0.0f)
-            return set_error(PBRT_ERR_UNSUPPORTED, "matte sigma != 0 (Oren-Nayar) is not supported");
     const char* names[3] = {"sah", "middle", "equal"};
     const char* sm = (d->split_method >= 0 && d->split_method < 3) ? names[d->split_method] : "sah";
     PbrtScene* S = new PbrtScene();
@@ -270,11 +267,20 @@ int pbrtgpu_scene_create(const PbrtSceneDesc* d, PbrtScene** out) {
         const uint32_t n_inner = (uint32_t)H.insts[H.spheres[p.sphere].instance].prims.size();
         S->inst_map.push_back(make_uint4(H.flat_id[i], (uint32_t)i, n_inner, (uint32_t)p.sphere));
     }
-    // matte Kd clamped to [0, f32::MAX] (matte.rs:42)
+    // MatteMaterial::get_bsdf (matte.rs:30-51): Kd clamped to [0, f32::MAX],
+    // sigma to [0, 90]; sigma == 0 -> Lambertian, else OrenNayar::new
+    // (orennayar.rs:15-28) with A and B computed here in f32
     for (uint32_t i = 0; i < d->n_materials; ++i) {
         const PbrtMaterialDesc& m = d->materials[i];
+        const float sig = clampf(m.sigma, 0.0f, 90.0f);
+        const float sigma = sig * 3.14159265358979323846f / 180.0f;  // utils/mod.rs:37-39
+        const float sigma2 = sigma * sigma;
+        const float a = 1.0f - (sigma2 / (2.0f * (sigma + 0.33f)));
+        const float b = 0.45f * sigma2 / (sigma2 + 0.09f);
+        const bool oren = !(sig == 0.0f);
         S->materials.push_back(make_float4(clampf(m.kd[0], 0.0f, FLT_MAX), clampf(m.kd[1], 0.0f, FLT_MAX),
-                                           clampf(m.kd[2], 0.0f, FLT_MAX), m.sigma));
+                                           clampf(m.kd[2], 0.0f, FLT_MAX), a));
+        S->materials.push_back(make_float4(b, bitsf(oren ? 1u : 0u), 0.0f, 0.0f));
     }
     for (uint32_t li = 0; li < d->n_lights; ++li) {
         const PbrtLightDesc& L = d->lights[li];

@@ -81,7 +81,7 @@ struct RenderParams {
     uint32_t has_wide;
     const ShadePrim* shade;
     const SphereRec* spheres;
-    const float4* materials;     // kd.rgb (clamped >= 0), sigma
+    const float4* materials;     // two per material: (kd.rgb clamped >= 0, Oren-Nayar A), (B, oren flag bits, 0, 0)
     const LightRec* lights;
     uint32_t n_lights;
     const AreaTri* area_tris;

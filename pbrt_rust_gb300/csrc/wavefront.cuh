@@ -256,11 +256,11 @@ __device__ __forceinline__ void segment(V p1, float eps1, V p2, float eps2, Pbrt
     r->tmax = (1.0f - eps2) * dist;
 }
 
-// Hit point and geometric normal of refined primitive `sp` (its analytic
-// record in `spheres`) for the ray (ro, rd) at t: the dg.p / dg.nn that the
-// shape's intersect builds.
+// Hit point, geometric normal and dp/du (world space) of refined primitive
+// `sp` (its analytic record in `spheres`) for the ray (ro, rd) at t: the
+// dg.p / dg.nn / dg.dpdu that the shape's intersect builds.
 __device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereRec* spheres, V ro, V rd, float t,
-                                              V* p_out, V* nn_out) {
+                                              V* p_out, V* nn_out, V* dpdu_out) {
     const uint32_t flags = __float_as_uint(sp.c[3]);
     V nn = mkv(0, 0, 1);
     if ((flags & kShadeSphere) && spheres[flags >> 2].kind != kQuadSphere) {
@@ -280,6 +280,11 @@ __device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereR
             nn = mkv(S.w2o[0] * 0.0f + S.w2o[4] * 0.0f + S.w2o[8] * nz,
                      S.w2o[1] * 0.0f + S.w2o[5] * 0.0f + S.w2o[9] * nz,
                      S.w2o[2] * 0.0f + S.w2o[6] * 0.0f + S.w2o[10] * nz);
+            const float k = S.phi_max / (2.0f * 3.14159265358979323846f);  // disk.rs:114-116
+            const V dpdu = vmul(mkv(-S.phi_max * ph.y, S.phi_max * ph.x, 0.0f), k);
+            float du[3];
+            xf_vector(S.o2w, dpdu.x, dpdu.y, dpdu.z, du);
+            *dpdu_out = ld3(du);
         } else {
             // cylinder.rs:143-164 + helpers.rs:17-43 + diff_geom.rs:52-79
             V dpdu = mkv(S.phi_max * -ph.y, S.phi_max * ph.x, 0.0f);
@@ -289,6 +294,7 @@ __device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereR
             xf_vector(S.o2w, dpdv.x, dpdv.y, dpdv.z, dv);
             nn = vnorm(vcross(ld3(du), ld3(dv)));
             if (S.flip) nn = vmul(nn, -1.0f);
+            *dpdu_out = ld3(du);
         }
     } else if (flags & kShadeSphere) {
         // sphere.rs:135-176 + shape/helpers.rs:17-43 + diff_geom.rs:52-79
@@ -313,6 +319,7 @@ __device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereR
         *p_out = ld3(pw);
         nn = vnorm(vcross(ld3(du), ld3(dv)));
         if (S.flip) nn = vmul(nn, -1.0f);
+        *dpdu_out = ld3(du);
     } else {
         // mesh.rs:212-264 with the default uvs: du1 = -1, du2 = 0,
         // dv1 = -1, dv2 = -1, determinant 1
@@ -325,8 +332,34 @@ __device__ __forceinline__ void surface_point(const ShadePrim& sp, const SphereR
         *p_out = mkv(ro.x + rd.x * t, ro.y + rd.y * t, ro.z + rd.z * t);
         nn = vnorm(vcross(dpdu, dpdv));
         if (flags & kShadeFlip) nn = vmul(nn, -1.0f);
+        *dpdu_out = dpdu;
     }
     *nn_out = nn;
+}
+
+// OrenNayar::f (orennayar.rs:31-62) without the reflectance: a + b *
+// maxcos * sin(alpha) * tan(beta) for local wo, wi (bsdf/utils.rs:5-28).
+__device__ __forceinline__ float sin_theta_l(V v) { return sqrtf(fmaxf(0.0f, 1.0f - v.z * v.z)); }
+__device__ __forceinline__ float clamp_unit(float x) { return x < -1.0f ? -1.0f : (x > 1.0f ? 1.0f : x); }
+__device__ __forceinline__ float oren_nayar_term(float a, float b, V wo, V wi) {
+    const float sinthetai = sin_theta_l(wi), sinthetao = sin_theta_l(wo);
+    float maxcos = 0.0f;
+    if (!(sinthetai < 1e-4f || sinthetao < 1e-4f)) {
+        const float cpi = sinthetai == 0.0f ? 1.0f : clamp_unit(wi.x / sinthetai);
+        const float spi = sinthetai == 0.0f ? 0.0f : clamp_unit(wi.y / sinthetai);
+        const float cpo = sinthetao == 0.0f ? 1.0f : clamp_unit(wo.x / sinthetao);
+        const float spo = sinthetao == 0.0f ? 0.0f : clamp_unit(wo.y / sinthetao);
+        maxcos = fmaxf(cpi * cpo + spi * spo, 0.0f);
+    }
+    float sinalpha, tanbeta;
+    if (fabsf(wi.z) > fabsf(wo.z)) {
+        sinalpha = sinthetao;
+        tanbeta = sinthetai / fabsf(wi.z);
+    } else {
+        sinalpha = sinthetai;
+        tanbeta = sinthetao / fabsf(wo.z);
+    }
+    return a + b * maxcos * sinalpha * tanbeta;
 }
 
 // Where shade_sample appends its shadow rays: the ray, the (sample, light)
@@ -351,9 +384,11 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
     float4 h = live ? P.hits[s] : make_float4(__int_as_float(-1), 0, 0, 0);
     int32_t prim = __float_as_int(h.x);
     bool hit = live && prim >= 0;
-    V p = mkv(0, 0, 0), nn = mkv(0, 0, 1), wo = mkv(0, 0, 1);
+    V p = mkv(0, 0, 0), nn = mkv(0, 0, 1), wo = mkv(0, 0, 1), dpdu = mkv(1, 0, 0);
     float eps = 0.0f;
     float kd[3] = {0, 0, 0};
+    float on_a = 0.0f, on_b = 0.0f;  // Oren-Nayar A, B (oren)
+    bool oren = false;
     float le[3] = {0, 0, 0};
     if (hit) {
         const PbrtRay r = P.rays[s];
@@ -394,13 +429,15 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
             }
         }
         const ShadePrim& sp = shade[id];
-        surface_point(sp, spheres, o, d, t, &p, &nn);
+        surface_point(sp, spheres, o, d, t, &p, &nn, &dpdu);
         if (inst) {
-            // transformed.rs:45-47: p by primitive-to-world, nn by its
-            // normal transform (w2p transposed), normalised
-            float pw[3];
+            // transformed.rs:45-49: p and dpdu by primitive-to-world, nn by
+            // its normal transform (w2p transposed), normalised
+            float pw[3], du[3];
             xf_point(inst->o2w, p.x, p.y, p.z, pw);
             p = ld3(pw);
+            xf_vector(inst->o2w, dpdu.x, dpdu.y, dpdu.z, du);
+            dpdu = ld3(du);
             const float* m = inst->w2o;
             nn = vnorm(mkv(m[0] * nn.x + m[4] * nn.y + m[8] * nn.z, m[1] * nn.x + m[5] * nn.y + m[9] * nn.z,
                            m[2] * nn.x + m[6] * nn.y + m[10] * nn.z));
@@ -416,10 +453,22 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
                 le[2] = L.spec[2];
             }
         }
-        float4 m = P.materials[__float_as_uint(sp.a[3])];
+        const uint32_t mi = __float_as_uint(sp.a[3]);
+        const float4 m = P.materials[2 * mi], m2 = P.materials[2 * mi + 1];
         kd[0] = m.x;
         kd[1] = m.y;
         kd[2] = m.z;
+        on_a = m.w;
+        on_b = m2.x;
+        oren = __float_as_uint(m2.y) != 0u;
+    }
+    // BSDF frame of Oren-Nayar (bsdf/mod.rs:70-86): tn = normalize(dpdu),
+    // sn = nn x tn, world_to_local(v) = (v.sn, v.tn, v.nn)
+    V tn = mkv(0, 0, 0), sn = mkv(0, 0, 0), wo_l = mkv(0, 0, 0);
+    if (oren) {
+        tn = vnorm(dpdu);
+        sn = vcross(nn, tn);
+        wo_l = mkv(vdot(wo, sn), vdot(wo, tn), vdot(wo, nn));
     }
     if (live) P.le[s] = make_float4(le[0], le[1], le[2], 0.0f);
     const float invpi = 1.0f / 3.14159265358979323846f;  // lambertian.rs:21
@@ -472,10 +521,15 @@ __device__ __forceinline__ void shade_sample(const RenderParams& P, uint64_t s, 
             if (!black && pdf != 0.0f) {
                 bool refl = vdot(wi, nn) * vdot(wo, nn) > 0.0f;  // bsdf/mod.rs:133-137
                 float f[3] = {0, 0, 0};
-                if (refl) {  // Lambertian::f (lambertian.rs:20-23)
+                if (refl && !oren) {  // Lambertian::f (lambertian.rs:20-23)
                     f[0] = kd[0] * invpi;
                     f[1] = kd[1] * invpi;
                     f[2] = kd[2] * invpi;
+                } else if (refl) {  // OrenNayar::f (orennayar.rs:31-62)
+                    const float g = oren_nayar_term(on_a, on_b, wo_l, mkv(vdot(wi, sn), vdot(wi, tn), vdot(wi, nn)));
+                    f[0] = kd[0] * invpi * g;
+                    f[1] = kd[1] * invpi * g;
+                    f[2] = kd[2] * invpi * g;
                 }
                 if (!(f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f)) {
                     float ad = fabsf(vdot(wi, nn));

@@ -160,3 +160,42 @@ def test_disk_and_cylinder_scene_matches_oracle(oracle):
         prims.append(Primitive.geometric(s, MatteMaterial((0.3 + 0.1 * i, 0.5, 0.7 - 0.1 * i))))
     gpu, ref = render_both(oracle, prims, lights, cam, smp)
     assert_image_close(gpu, ref)
+
+
+def test_oren_nayar_triangle_scene_is_bit_exact(oracle):
+    """Matte with sigma > 0 is Oren-Nayar (matte.rs:42-47, orennayar.rs):
+    its frame comes from dp/du; triangle-only scenes stay exact IEEE f32."""
+    prims, lights, cam, smp = G.c1_scene(res=96, n_spheres=0)
+    soup = G.ray_soup(400, 1, seed=6)[0]
+    for i, p in enumerate(soup):
+        p.material = MatteMaterial((0.3 + 0.001 * i, 0.6, 0.4), sigma=(5.0, 20.0, 60.0, 90.0, 150.0)[i % 5])
+    prims[0].material = MatteMaterial((0.5, 0.5, 0.5), sigma=35.0)
+    prims += soup
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
+    assert ref.max() > 0.1
+
+
+def test_oren_nayar_quadrics_and_instances_match_oracle(oracle):
+    """dp/du of spheres, disks (with the phi_max / 2 pi factor of
+    disk.rs:114-116) and cylinders, and of instance hits moved by
+    primitive-to-world (transformed.rs:48)."""
+    from pbrt_rust_gb300.scene import InstanceDefinition, Primitive, Shape
+    from pbrt_rust_gb300.transform import Transform
+    prims, lights, cam, smp = G.c1_scene(res=64, n_spheres=10)
+    for i, p in enumerate(prims[1:11]):
+        p.material = MatteMaterial(p.material.kd, sigma=15.0 + 7.0 * i)
+    for i in range(4):
+        t = Transform.translate((i - 1.5, 0.6, -1.0)) * Transform.rotate(-90.0 + 30.0 * i, (1, 0, 0))
+        s = (Shape.disk(t, None, False, 0.0, 0.45, 0.1, 300.0) if i % 2
+             else Shape.cylinder(t, None, False, 0.3, -0.4, 0.4, 360.0))
+        prims.append(Primitive.geometric(s, MatteMaterial((0.6, 0.4, 0.3), sigma=40.0)))
+    defn = InstanceDefinition([
+        Primitive.geometric(Shape.sphere(Transform(), None, False, 0.3, -0.3, 0.3, 360.0), MatteMaterial((0.7,) * 3, 25.0)),
+        Primitive.geometric(Shape.disk(Transform.translate((0.0, 0.0, -0.3)), None, False, 0.0, 0.4, 0.0, 360.0),
+                            MatteMaterial((0.2, 0.7, 0.3), 50.0))])
+    for k in range(3):
+        i2w = Transform.translate((-1.0 + k, 1.6, 1.0)) * Transform.rotate(40.0 * k, (0, 1, 0)) * Transform.scale(1.3, 1.3, 1.3)
+        prims.append(Primitive.transformed(defn, i2w.inverse()))
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert_image_close(gpu, ref)
