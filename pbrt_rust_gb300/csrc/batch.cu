@@ -49,7 +49,7 @@ __device__ __forceinline__ uint32_t locate(const uint64_t* __restrict__ off, uin
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_generate(BatchArgs A) {
-    __shared__ uint32_t words[16 * BLOCK];  // the threads' ChaCha blocks
+    __shared__ uint32_t words[32 * BLOCK];  // the threads' ChaCha block pairs
     const uint64_t total = A.hdr->pix;
     const uint32_t nj = A.hdr->n_jobs;
     Cursor c{0, 1, 0};

@@ -63,17 +63,63 @@ __device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr
     out[14u * stride] = x14;
     out[15u * stride] = x15;
 }
+// Blocks ctr and ctr + 1 at once (two independent chains for the
+// scheduler): word k of block ctr + j at out[(16 j + k) * stride].
+__device__ __forceinline__ void chacha12_block2(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride) {
+    const uint64_t c1 = ctr + 1;
+    uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
+    uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
+    uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
+    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = 0u, x15 = 0u;
+    uint32_t y0 = 0x61707865u, y1 = 0x3320646eu, y2 = 0x79622d32u, y3 = 0x6b206574u;
+    uint32_t y4 = key[0], y5 = key[1], y6 = key[2], y7 = key[3];
+    uint32_t y8 = key[4], y9 = key[5], y10 = key[6], y11 = key[7];
+    uint32_t y12 = (uint32_t)c1, y13 = (uint32_t)(c1 >> 32), y14 = 0u, y15 = 0u;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        PBRT_QR(x0, x4, x8, x12);
+        PBRT_QR(y0, y4, y8, y12);
+        PBRT_QR(x1, x5, x9, x13);
+        PBRT_QR(y1, y5, y9, y13);
+        PBRT_QR(x2, x6, x10, x14);
+        PBRT_QR(y2, y6, y10, y14);
+        PBRT_QR(x3, x7, x11, x15);
+        PBRT_QR(y3, y7, y11, y15);
+        PBRT_QR(x0, x5, x10, x15);
+        PBRT_QR(y0, y5, y10, y15);
+        PBRT_QR(x1, x6, x11, x12);
+        PBRT_QR(y1, y6, y11, y12);
+        PBRT_QR(x2, x7, x8, x13);
+        PBRT_QR(y2, y7, y8, y13);
+        PBRT_QR(x3, x4, x9, x14);
+        PBRT_QR(y3, y4, y9, y14);
+    }
+    const uint32_t xs[16] = {x0 + 0x61707865u, x1 + 0x3320646eu, x2 + 0x79622d32u, x3 + 0x6b206574u,
+                             x4 + key[0],      x5 + key[1],      x6 + key[2],      x7 + key[3],
+                             x8 + key[4],      x9 + key[5],      x10 + key[6],     x11 + key[7],
+                             x12 + (uint32_t)ctr, x13 + (uint32_t)(ctr >> 32), x14, x15};
+    const uint32_t ys[16] = {y0 + 0x61707865u, y1 + 0x3320646eu, y2 + 0x79622d32u, y3 + 0x6b206574u,
+                             y4 + key[0],      y5 + key[1],      y6 + key[2],      y7 + key[3],
+                             y8 + key[4],      y9 + key[5],      y10 + key[6],     y11 + key[7],
+                             y12 + (uint32_t)c1, y13 + (uint32_t)(c1 >> 32), y14, y15};
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        out[(uint32_t)k * stride] = xs[k];
+        out[(uint32_t)(16 + k) * stride] = ys[k];
+    }
+}
 #undef PBRT_QR
 
-// A seekable reader of one task's word stream.  Blocks are computed when a
-// word of them is read, so words skipped over (whole blocks of them) cost
-// nothing.  The current block lives in the caller's shared-memory column
+// A seekable reader of one task's word stream.  Blocks are computed in
+// pairs (two independent chains keep the scheduler busy) when a word of
+// them is read, so words skipped over (whole pairs of blocks) cost nothing.
+// The current pair lives in the caller's shared-memory column of 32 words
 // (word k at buf[k * stride]): a per-thread array would go to local memory,
 // whose loads and stores throttle the generate kernels.
 struct WordStream {
     uint32_t key[8];
     uint64_t block;   // block of the next word
-    uint64_t loaded;  // block held in buf (~0: none)
+    uint64_t loaded;  // first block of the pair held in buf (~1: none, so block - loaded > 1)
     uint32_t* buf;
     uint32_t stride;
     int idx;          // next word inside `block` (16: the block is used up)
@@ -83,7 +129,7 @@ struct WordStream {
         for (int i = 0; i < 8; ++i) key[i] = k[i];
         block = word >> 4;
         idx = (int)(word & 15);
-        loaded = ~0ull;
+        loaded = ~1ull;
         buf = column;
         stride = column_stride;
     }
@@ -98,11 +144,11 @@ struct WordStream {
             ++block;
             idx = 0;
         }
-        if (block != loaded) {
-            chacha12_block(key, block, buf, stride);
+        if (block - loaded > 1u) {  // not in the pair held (also when none is)
+            chacha12_block2(key, block, buf, stride);
             loaded = block;
         }
-        return buf[(uint32_t)idx++ * stride];
+        return buf[((uint32_t)(block - loaded) * 16u + (uint32_t)idx++) * stride];
     }
     __device__ __forceinline__ uint64_t next_u64() {  // low word first
         uint64_t lo = next_u32();

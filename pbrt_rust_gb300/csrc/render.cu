@@ -24,7 +24,7 @@
 namespace pbrt {
 
 __global__ void __launch_bounds__(128) k_generate(RenderParams P) {
-    __shared__ uint32_t words[16 * 128];  // the threads' ChaCha blocks
+    __shared__ uint32_t words[32 * 128];  // the threads' ChaCha block pairs
     uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= P.n_pixels) return;
     generate_pixel(P, pix, words + threadIdx.x, 128u);

@@ -106,7 +106,7 @@ __device__ __forceinline__ void camera_ray(const RenderParams& P, const float* r
 }
 
 // One sampler pixel (k_generate's item).  `rng_col`: this thread's column
-// of 16 words in shared memory (word k at rng_col[k * stride]).
+// of 32 words in shared memory (word k at rng_col[k * stride]).
 __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t pix, uint32_t* rng_col,
                                                uint32_t stride) {
     int32_t sw = P.sx1 - P.sx0;
