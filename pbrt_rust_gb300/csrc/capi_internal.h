@@ -102,6 +102,9 @@ namespace pbrt {
 // per-render buffers (capi_render.cu).
 int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp, uint32_t task_lo,
                    uint32_t task_hi, RenderParams* out, std::vector<TaskRec>* tasks);
+// The scene's fields of RenderParams (BVH layouts, shading tables, lights,
+// instances); the scene is uploaded (capi_render.cu).
+void scene_params(const PbrtScene* S, RenderParams* P);
 // Render set-up helpers (capi_render.cu), the reference's f32 arithmetic.
 int32_t f2i32(float f);
 size_t f2usize(float f);

@@ -197,21 +197,7 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     P.filter_table = (const float*)p_table;
     P.tasks = (const TaskRec*)p_tasks;
     P.n_tasks = smp->num_tasks;
-    P.bvh = S->bvh->dev;
-    P.depth = S->bvh->host.depth;
-    P.bvh4 = S->bvh->dev4;
-    P.wide_bound = S->bvh->host.stack4_bound;
-    P.has_wide = wide_of(S->bvh) ? 1u : 0u;
-    P.shade = S->d_shade;
-    P.spheres = S->bvh->d_spheres;
-    P.materials = S->d_materials;
-    P.lights = S->d_lights;
-    P.n_lights = nl;
-    P.area_tris = S->d_area_tris;
-    P.area_cdf = S->d_area_cdf;
-    P.n_inst = (uint32_t)S->inst_map.size();
-    P.inst_map = S->d_inst_map;
-    P.inst_defs = S->d_inst_defs;
+    scene_params(S, &P);
     P.rays = (PbrtRay*)p_rays;
     P.hits = (float4*)p_hits;
     P.img = (float2*)p_img;

@@ -174,6 +174,24 @@ static inline float bitsf(uint32_t u) {
     return f;
 }
 
+void scene_params(const PbrtScene* S, RenderParams* P) {
+    P->bvh = S->bvh->dev;
+    P->depth = S->bvh->host.depth;
+    P->bvh4 = S->bvh->dev4;
+    P->wide_bound = S->bvh->host.stack4_bound;
+    P->has_wide = wide_of(S->bvh) ? 1u : 0u;
+    P->shade = S->d_shade;
+    P->spheres = S->bvh->d_spheres;
+    P->materials = S->d_materials;
+    P->lights = S->d_lights;
+    P->n_lights = (uint32_t)S->lights.size();
+    P->area_tris = S->d_area_tris;
+    P->area_cdf = S->d_area_cdf;
+    P->n_inst = (uint32_t)S->inst_map.size();
+    P->inst_map = S->d_inst_map;
+    P->inst_defs = S->d_inst_defs;
+}
+
 // Per refined primitive shading records (ShadePrim) of one BVH.
 static void shade_records(const HostBVH& H, std::vector<ShadePrim>* out) {
     out->resize(H.prims.size());
@@ -466,21 +484,7 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
         T.fy0 = std::max(te[2], P.fy0);
         T.fy1 = std::min(te[3], P.fy1);
     }
-    P.bvh = S->bvh->dev;
-    P.depth = S->bvh->host.depth;
-    P.bvh4 = S->bvh->dev4;
-    P.wide_bound = S->bvh->host.stack4_bound;
-    P.has_wide = wide_of(S->bvh) ? 1u : 0u;
-    P.shade = S->d_shade;
-    P.spheres = S->bvh->d_spheres;
-    P.materials = S->d_materials;
-    P.lights = S->d_lights;
-    P.n_lights = nl;
-    P.area_tris = S->d_area_tris;
-    P.area_cdf = S->d_area_cdf;
-    P.n_inst = (uint32_t)S->inst_map.size();
-    P.inst_map = S->d_inst_map;
-    P.inst_defs = S->d_inst_defs;
+    scene_params(S, &P);
     *out = P;
     *tasks_out = std::move(tasks);
     return PBRT_OK;

@@ -70,3 +70,21 @@ def test_instanced_render_in_a_batch_equals_the_single_render():
     assert np.array_equal(out[0].view(np.uint32), alone.view(np.uint32))
     assert np.array_equal(out[1].view(np.uint32), alone2.view(np.uint32))
     assert np.array_equal(out[2].view(np.uint32), bvh.intersect(queries).view(np.uint32))
+
+
+def test_oren_nayar_instanced_batch_equals_the_single_render():
+    """Oren-Nayar materials inside instance definitions, rendered alone and
+    in a batch next to a query of the same aggregate."""
+    prims, lights, cam, smp, _ = G.instanced_forest(n_instances=10, tris_per_tree=200, seed=8, res=48)
+    for p in prims[1:-1]:
+        for q in p.shape.definition.prims:
+            q.material = type(q.material)(q.material.kd, sigma=30.0)
+    sc = GpuScene(prims, lights)
+    nt = default_num_tasks(48, 48)
+    r = GpuSamplerRenderer(smp, cam, num_tasks=nt)
+    alone = r.render(sc)
+    batch = GpuBatch(max_jobs=4, max_samples=1 << 15)
+    batch.add_render(sc, r)
+    out = batch.run()
+    assert np.array_equal(out[0].view(np.uint32), alone.view(np.uint32))
+    assert alone.max() > 0.05
