@@ -319,6 +319,35 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 400, 
             "poisson_mean_batch": poisson["mean_batch_requests"], "bit_exact": exact}
 
 
+def bench_rmse(torch, dev, stream):
+    """The plain render config (512x512, 2x2 strata, ground, 64 spheres,
+    point + area light): frame time and RMSE (linear RGB) against the same
+    scene at 8x8 strata (64 spp, the most a pixel takes; same task split, so
+    the same task seams), whose own noise adds about 3 % to the figure.  The
+    batched and served forms produce bit-identical images, hence the same
+    RMSE."""
+    from pbrt_rust_gb300 import generators as G
+    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
+    prims, lights, cam, smp = G.c1_scene(res=512)
+    scene = GpuScene(prims, lights)
+    img = torch.empty((512, 512, 3), dtype=torch.float32, device=dev)
+    r4 = GpuSamplerRenderer(smp, cam)
+    r4.render(scene, out=img, stream=stream)
+    t = []
+    for _ in range(5):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r4.render(scene, out=img, stream=stream)
+        t.append(time.perf_counter() - t0)
+    _, _, _, smp64 = G.c1_scene(res=512, spp_side=8)
+    ref = torch.empty_like(img)
+    GpuSamplerRenderer(smp64, cam).render(scene, out=ref, stream=stream)
+    torch.cuda.synchronize(dev)
+    rmse = float(torch.sqrt(torch.mean((img - ref) ** 2)).item())
+    return {"ms_mean": 1e3 * statistics.mean(t), "ms_min": 1e3 * min(t), "spp": 4, "rmse_vs_64spp": rmse,
+            "reference_mean": float(ref.mean().item())}
+
+
 def bench_instanced(torch, dev, stream, n_instances: int = 256, tris_per_tree: int = 20000,
                     n_rays: int = 1 << 22):
     """TransformedPrimitive instancing: the instanced forest against the
@@ -502,6 +531,7 @@ def run_ours(args):
         renderer.render(scene, out=img, stream=stream)
         rt.append(time.perf_counter() - t0)
     instanced = bench_instanced(torch, dev, stream)
+    c1 = bench_rmse(torch, dev, stream)
     batched = bench_batched(torch, dev, stream) if not args.skip_multi else None
     served = bench_served(torch, dev, stream) if not args.skip_multi else None
     clk.__exit__(None, None, None)
@@ -544,6 +574,7 @@ def run_ours(args):
             "any_hit": {"value": N_RAYS / (statistics.mean(ms_any) / 1e3) / 1e6, "unit": "Mrays/s"},
             "render_1024x1024_16spp": {"ms_mean": 1e3 * statistics.mean(rt), "ms_min": 1e3 * min(rt),
                                        "camera_rays": 1024 * 1024 * 16},
+            "render_c1_512x512_4spp": c1,
             "bvh_build": {"host_s": build_s, "device_s": dbuild_s, "identical": same_tree,
                           "what": "pbrtgpu_bvh_create(_ex) of the 1M-triangle heightfield, host vs device tree build"},
             "instancing": instanced,
