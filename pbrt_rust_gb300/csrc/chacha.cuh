@@ -110,6 +110,16 @@ __device__ __forceinline__ void chacha12_block2(const uint32_t* key, uint64_t ct
 }
 #undef PBRT_QR
 
+// The one copy of the pair computation in a kernel (each inlined read site
+// would otherwise carry its own ~1200 instructions); the key goes by value
+// so that it stays in registers.
+static __device__ __noinline__ void chacha12_fill2(uint32_t k0, uint32_t k1, uint32_t k2, uint32_t k3, uint32_t k4,
+                                                   uint32_t k5, uint32_t k6, uint32_t k7, uint64_t ctr,
+                                                   uint32_t* out, uint32_t stride) {
+    const uint32_t key[8] = {k0, k1, k2, k3, k4, k5, k6, k7};
+    chacha12_block2(key, ctr, out, stride);
+}
+
 // A seekable reader of one task's word stream.  Blocks are computed in
 // pairs (two independent chains keep the scheduler busy) when a word of
 // them is read, so words skipped over (whole pairs of blocks) cost nothing.
@@ -145,7 +155,7 @@ struct WordStream {
             idx = 0;
         }
         if (block - loaded > 1u) {  // not in the pair held (also when none is)
-            chacha12_block2(key, block, buf, stride);
+            chacha12_fill2(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], block, buf, stride);
             loaded = block;
         }
         return buf[((uint32_t)(block - loaded) * 16u + (uint32_t)idx++) * stride];
