@@ -359,9 +359,9 @@ struct Traversal {
     bool found;
     bool nan_hit;  // a NaN-distance hit was accepted: the result needs an EXACT replay
     TraceResult res;
-    uint32_t st_a[STACK];
-    uint32_t st_b[STACK];
-    float st_t[STACK];
+    // deferred children: (a, b, entry distance bits, unused) - one 16-byte
+    // local store and load per entry instead of three
+    uint4 st[STACK];
 
     __device__ __forceinline__ bool start(const DevBVH& bvh, const DRay& r) {
         maxt = r.tmax;
@@ -446,9 +446,7 @@ struct Traversal {
                         *status = 6;
                         return false;
                     }
-                    st_a[sp] = fa;
-                    st_b[sp] = fb;
-                    st_t[sp] = tf;
+                    st[sp] = make_uint4(fa, fb, __float_as_uint(tf), 0u);
                     ++sp;
                 }
                 a = na;
@@ -461,12 +459,15 @@ struct Traversal {
                 return true;
             }
         }
-        // pop the next deferred child whose box still passes
+        // pop the next deferred child whose box still passes; an any-hit
+        // walk ends at its first hit, so its maxt is the one the child was
+        // pushed against and the child passes without the check
         while (sp > 0) {
             --sp;
-            if (!(st_t[sp] > maxt)) {
-                a = st_a[sp];
-                b = st_b[sp];
+            const uint4 e = st[sp];
+            if ((ANY && !EXACT) || !(__uint_as_float(e.z) > maxt)) {
+                a = e.x;
+                b = e.y;
                 return true;
             }
         }
