@@ -227,7 +227,28 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
     return st;
 }
 
-// Host-buffer calls of at least 2 * kPipeChunkMin rays run in
+// Pinned host memory is mapped into the device's address space (on GB300
+// it is the Grace memory behind NVLink-C2C): the traversal then reads the
+// rays and writes the results there directly, with no staging copies.
+// Measured with 2^22 heightfield rays in pinned buffers: closest hit 1.63 ms
+// against 1.75 ms through the copy pipeline below, any hit 1.24 against
+// 1.43 ms, identical results.  PBRT_HOST_MAPPED=0 (read at every call)
+// takes the copy pipeline.
+static bool host_mapped_enabled() {
+    const char* v = getenv("PBRT_HOST_MAPPED");
+    return !(v && v[0] == '0');
+}
+// The device address of a pinned, mapped host allocation, else nullptr.
+static void* mapped_host_pointer(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Other host-buffer calls of at least 2 * kPipeChunkMin rays run in
 // pipe_chunks() chunks (PBRT_PIPE_CHUNKS: 1 = one piece, at most
 // kPipeChunks; default 4) whose copies overlap the other chunks' traversal;
 // consecutive chunks trace on two streams so that one kernel's tail overlaps
@@ -274,6 +295,16 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
     size_t out_bytes = hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n;
     bool dr = is_device_pointer(rays), dout = is_device_pointer(out);
     if (dr && dout) return launch_batch(b, rays, n, hits, occ, s);
+    if (host_mapped_enabled()) {
+        const void* mr = dr ? (const void*)rays : mapped_host_pointer(rays);
+        void* mo = dout ? out : mapped_host_pointer(out);
+        if (mr && mo) {
+            if ((st = launch_batch(b, static_cast<const PbrtRay*>(mr), n, hits ? static_cast<PbrtHit*>(mo) : nullptr,
+                                   hits ? nullptr : static_cast<uint8_t*>(mo), s)))
+                return st;
+            return cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        }
+    }
     std::lock_guard<std::mutex> lk(b->stage_mu);
     const PbrtRay* d_rays = rays;
     if (!dr) {

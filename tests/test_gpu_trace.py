@@ -387,3 +387,30 @@ def test_pipelined_host_buffers_equal_device_buffers():
     out = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory()
     g.intersect(pinned, out=out)
     assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+
+
+@pytest.mark.gpu
+def test_pinned_host_buffers_in_place_and_staged(monkeypatch):
+    """Pinned host buffers are read and written in place by the traversal
+    (mapped host memory); PBRT_HOST_MAPPED=0 stages them through device
+    copies instead.  Both, and a pinned/device mix, give the device-buffer
+    results bit for bit."""
+    torch = _torch()
+    prims, _ = G.ray_soup(4096, 1, seed=5)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    rays = G.incoherent_rays(G.PCG32(37), (1 << 19) + 777, lo, hi)
+    want, want_any = dev_hits(g, rays), dev_any(g, rays)
+    assert (want["prim"] >= 0).sum() > 5000
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    for mode in ("1", "0"):
+        monkeypatch.setenv("PBRT_HOST_MAPPED", mode)
+        out = torch.full((len(rays), 4), 7.0, dtype=torch.float32).pin_memory()
+        g.intersect(pinned, out=out)
+        assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1)), mode
+        occ = torch.full((len(rays),), 9, dtype=torch.uint8).pin_memory()
+        g.intersect_p(pinned, out=occ)
+        assert np.array_equal(occ.numpy(), want_any), mode
+        dout = torch.full((len(rays), 4), 7.0, dtype=torch.float32, device="cuda")
+        g.intersect(pinned, out=dout)
+        assert np.array_equal(dout.cpu().numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1)), mode
