@@ -134,3 +134,24 @@ def test_autotune_keeps_results(jobs):
     tuned, ms = b.autotune(repeats=1)
     assert ms > 0 and tuned["block"] in (128, 256)
     check(b.run(), scenes, queries)
+
+
+def test_thin_lens_jobs_equal_single_renders(oracle):
+    """Thin-lens cameras (the sampler's general path) in one batch, with odd
+    and even sample counts so that jobs start on both halves of a 16-byte
+    film-position pair: each job equals its single render and the oracle."""
+    from pbrt_rust_gb300.scene import Camera, StratifiedSampler
+    b = GpuBatch(max_jobs=4, max_samples=1 << 18)
+    want = []
+    for res, side in ((33, 1), (40, 3), (24, 2)):
+        prims, lights, cam0, _ = G.c1_scene(res=res, n_spheres=0)
+        cam = Camera.perspective(cam0.camera_to_world, cam0.screen_window, 0.0, 1.0, 0.08, 5.5, cam0.fov, cam0.film)
+        smp = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
+        sc, r = GpuScene(prims, lights, 4, "sah"), GpuSamplerRenderer(smp, cam)
+        single = r.render(sc)
+        ref = oracle.render(SceneDescription(prims, lights, 4, "sah"), cam, smp, r.num_tasks)
+        assert np.array_equal(single.view(np.uint32), ref.view(np.uint32))
+        b.add_render(sc, r)
+        want.append(single)
+    for got, w in zip(b.run(), want):
+        assert np.array_equal(bits(got), bits(w))

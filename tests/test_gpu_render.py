@@ -49,6 +49,30 @@ def test_triangle_scene_is_bit_exact(oracle):
     assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
 
 
+def thin_lens_case(res=72, xs=3, ys=3):
+    """A triangle-only C1 scene through a thin-lens camera (lens radius
+    0.08, focal distance 5.5): the sampler's general path with its lens and
+    time strata and their shuffles (projective.rs:79-96)."""
+    prims, lights, cam0, _ = G.c1_scene(res=res, n_spheres=0)
+    prims += G.ray_soup(300, 1, seed=7)[0]
+    cam = Camera.perspective(cam0.camera_to_world, cam0.screen_window, 0.0, 1.0, 0.08, 5.5, cam0.fov, cam0.film)
+    smp = StratifiedSampler.stratified(0, res, 0, res, xs, ys, True, 0.0, 1.0)
+    return prims, lights, cam, smp
+
+
+@pytest.mark.parametrize("xs,ys", [(3, 3), (2, 2), (1, 1)])
+def test_thin_lens_camera_is_bit_exact(oracle, xs, ys):
+    """Odd and even sample counts per pixel through the thin lens; without
+    spheres every step is exact f32, so the images are equal."""
+    prims, lights, cam, smp = thin_lens_case(xs=xs, ys=ys)
+    gpu, ref = render_both(oracle, prims, lights, cam, smp)
+    assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))
+    pin = render_both(oracle, *thin_lens_case(xs=xs, ys=ys)[:2],
+                      Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, cam.fov,
+                                         cam.film), smp)[1]
+    assert not np.array_equal(ref, pin)  # the lens changes the image
+
+
 @pytest.mark.parametrize("xs,ys,jitter,tasks", [(1, 1, True, 8), (4, 4, True, 3), (3, 2, False, 5), (2, 2, True, 1)])
 def test_sampler_variants(oracle, xs, ys, jitter, tasks):
     prims, lights, cam, _ = G.c1_scene(res=80)
