@@ -119,22 +119,36 @@ static __device__ __noinline__ void chacha12_fill2(uint32_t k0, uint32_t k1, uin
     const uint32_t key[8] = {k0, k1, k2, k3, k4, k5, k6, k7};
     chacha12_block2(key, ctr, out, stride);
 }
+// The last block of a reader's range alone (the pair's second block would
+// belong to the next reader): 0.473 -> 0.455 ms for 1024^2 x 16 samples.
+static __device__ __noinline__ void chacha12_fill1(uint32_t k0, uint32_t k1, uint32_t k2, uint32_t k3, uint32_t k4,
+                                                   uint32_t k5, uint32_t k6, uint32_t k7, uint64_t ctr,
+                                                   uint32_t* out, uint32_t stride) {
+    const uint32_t key[8] = {k0, k1, k2, k3, k4, k5, k6, k7};
+    chacha12_block(key, ctr, out, stride);
+}
 
 // A seekable reader of one task's word stream.  Blocks are computed in
 // pairs (two independent chains keep the scheduler busy) when a word of
-// them is read, so words skipped over (whole pairs of blocks) cost nothing.
+// them is read, so words skipped over (whole pairs of blocks) cost nothing;
+// the last block of the reader's range [word, end_word) is computed alone.
 // The current pair lives in the caller's shared-memory column of 32 words
 // (word k at buf[k * stride]): a per-thread array would go to local memory,
 // whose loads and stores throttle the generate kernels.
 struct WordStream {
     uint32_t key[8];
     uint64_t block;   // block of the next word
-    uint64_t loaded;  // first block of the pair held in buf (~1: none, so block - loaded > 1)
+    uint64_t loaded;  // first block held in buf (~1: none, so block - loaded >= span)
+    uint64_t end;     // first block past the reader's words
+    uint32_t span;    // blocks held in buf: 2, or 1 for the range's last block
     uint32_t* buf;
     uint32_t stride;
     int idx;          // next word inside `block` (16: the block is used up)
 
-    __device__ void seek(const uint32_t* k, uint64_t word, uint32_t* column, uint32_t column_stride) {
+    __device__ void seek(const uint32_t* k, uint64_t word, uint64_t end_word, uint32_t* column,
+                         uint32_t column_stride) {
+        end = (end_word + 15) >> 4;
+        span = 2;
 #pragma unroll
         for (int i = 0; i < 8; ++i) key[i] = k[i];
         block = word >> 4;
@@ -154,8 +168,12 @@ struct WordStream {
             ++block;
             idx = 0;
         }
-        if (block - loaded > 1u) {  // not in the pair held (also when none is)
-            chacha12_fill2(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], block, buf, stride);
+        if (block - loaded >= span) {  // not among the blocks held (also when none is)
+            span = block + 1 < end ? 2u : 1u;
+            if (span == 2u)
+                chacha12_fill2(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], block, buf, stride);
+            else
+                chacha12_fill1(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], block, buf, stride);
             loaded = block;
         }
         return buf[((uint32_t)(block - loaded) * 16u + (uint32_t)idx++) * stride];

@@ -167,7 +167,7 @@ __device__ __forceinline__ void generate_pixel(const RenderParams& P, uint32_t p
     const TaskRec& T = P.tasks[t];
     uint64_t j = (uint64_t)(y - T.wy0) * (uint64_t)(T.wx1 - T.wx0) + (uint64_t)(x - T.wx0);
     WordStream rng;
-    rng.seek(T.key, j * P.words_per_pixel, rng_col, stride);
+    rng.seek(T.key, j * P.words_per_pixel, (j + 1) * P.words_per_pixel, rng_col, stride);
     const bool jit = P.jitter != 0;
     if (!(P.lens_radius > 0.0f)) {
         // Pinhole camera: the ray depends on the image position alone, so
