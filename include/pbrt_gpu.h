@@ -397,7 +397,8 @@ typedef struct PbrtBatchTuning {
     uint32_t block;         /* threads per block: 128 or 256 */
     uint32_t stack;         /* 4-wide kernels: shared-memory stack entries per ray, 8 or 16 */
     uint32_t chunk;         /* rays a warp takes from the work counter at a time: 32..4096, multiple of 32 */
-    uint32_t refill;        /* extend: refill a warp when this many lanes are idle, 1..32 */
+    uint32_t refill;        /* extend: refill a warp when this many lanes are idle, 1..32;
+                               32: each lane walks its ray to the end, no per-step vote */
     uint32_t refill_shadow; /* shadow: same, 1..32 */
     uint32_t use_graph;     /* 1: replay the stage sequence as one CUDA graph */
 } PbrtBatchTuning;
