@@ -2,10 +2,15 @@
 
   python -m pbrt_rust_gb300.profile trace  [--rays N] [--any] [--repeat R]
   python -m pbrt_rust_gb300.profile render [--res R] [--spp-side S] [--repeat R]
+  python -m pbrt_rust_gb300.profile batch  [--scenes N] [--repeat R]
 
-Both use the 708x708 heightfield scene; `trace` runs R closest-hit (or
-any-hit) passes over N incoherent rays, `render` R frames of the direct-
-lighting wavefront.  Each pass is timed with CUDA events on its stream.
+`trace` and `render` use the 708x708 heightfield scene; `trace` runs R
+closest-hit (or any-hit) passes over N incoherent rays, `render` R frames of
+the direct-lighting wavefront.  `batch` renders the multi-scene workload
+(N scenes of 1k-256k triangles + 0-32 spheres, 128-512 squared, 1/4/16 spp)
+as one batch R times, with the tuning the autotuner picks for it (binary
+walks, 256 threads, refill 32: the flat traversal stages).  Each pass is
+timed with CUDA events on its stream.
 """
 from __future__ import annotations
 
@@ -18,7 +23,8 @@ import numpy as np
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["trace", "render"])
+    ap.add_argument("what", choices=["trace", "render", "batch"])
+    ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--rays", type=int, default=1 << 20)
     ap.add_argument("--any", action="store_true")
     ap.add_argument("--repeat", type=int, default=3)
@@ -35,8 +41,37 @@ def main(argv=None) -> int:
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     sh = C.c_void_p(stream.cuda_stream)
-    prims, lights, cam, smp, rays = G.heightfield(n_rays=a.rays if a.what == "trace" else 0)
     times = []
+    if a.what == "batch":
+        from concurrent.futures import ThreadPoolExecutor
+
+        from .batch import GpuBatch
+
+        def one(i):
+            p, li, c, sm = G.multi_scene(i)
+            return GpuScene(p, li), GpuSamplerRenderer(sm, c)
+
+        with ThreadPoolExecutor(8) as ex:  # host BVH builds release the GIL
+            items = list(ex.map(one, range(a.scenes)))
+        px = [r.camera.film.x_res * r.camera.film.y_res for _, r in items]
+        samples = sum(n * r.sampler.x_samples * r.sampler.y_samples for n, (_, r) in zip(px, items))
+        b = GpuBatch(max_jobs=a.scenes, max_tasks=64 * a.scenes, max_samples=samples,
+                     max_light_samples=2 * samples, max_film_pixels=sum(px))
+        b.set_tuning(extend_kernel="pair", shadow_kernel="pair", block=256, chunk=64, refill=32, refill_shadow=32,
+                     use_graph=1)
+        outs = [torch.empty((r.camera.film.y_res, r.camera.film.x_res, 3), device="cuda") for _, r in items]
+        for _ in range(a.repeat):
+            for (sc, r), o in zip(items, outs):
+                b.add_render(sc, r, out=o)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.launch(stream)
+            e1.record(stream)
+            b.wait()
+            times.append(e0.elapsed_time(e1))
+        print(f"batch: {' '.join(f'{t:.3f}' for t in times)} ms; best {a.scenes / (min(times) / 1e3):.0f} renders/s")
+        return 0
+    prims, lights, cam, smp, rays = G.heightfield(n_rays=a.rays if a.what == "trace" else 0)
     if a.what == "trace":
         bvh = GpuBVHAccel(prims, 4, "sah")
         rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
