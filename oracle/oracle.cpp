@@ -8,8 +8,8 @@
 //
 // Only tests/, __graft_entry__.smoke() and the benchmark's CPU baseline
 // use this library.  Where the reference is stubbed or buggy on the path,
-// the decision taken is written beside the code (D-numbers match the
-// table in the design doc).
+// the decision taken is written beside the code, each with a D-number that
+// the device code uses for the same decision.
 #include "oracle.h"
 
 #include <algorithm>
