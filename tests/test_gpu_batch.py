@@ -86,6 +86,7 @@ def test_batch_render_matches_oracle(jobs, oracle):
     dict(extend_kernel="wide", shadow_kernel="pair", stack=8, block=256),
     dict(extend_kernel="pair", shadow_kernel="wide", chunk=32, refill=4, refill_shadow=4),
     dict(block=256, chunk=256, refill=1, refill_shadow=16, use_graph=0),
+    dict(extend_kernel="pair", shadow_kernel="pair", block=256, chunk=96, refill=32, refill_shadow=32),
 ])
 def test_every_tuning_gives_the_same_outputs(jobs, tune):
     scenes, queries = jobs
