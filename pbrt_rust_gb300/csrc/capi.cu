@@ -191,7 +191,7 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
     const bool reorder = trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
     const bool chunked = trace_chunk() != 0;
     // [256 B: chunk counter, replay flag][permutation scratch]
-    cudaMemPool_t pool;
+    cudaMemPool_t pool = nullptr;
     if ((st = scratch_pool(b->device, &pool))) return st;
     const size_t bytes = 256 + (reorder ? ray_order_scratch_bytes(n) : 0);
     if ((st = cuda_status(cudaMallocFromPoolAsync(&scratch, bytes, pool, s), "cudaMallocFromPoolAsync"))) return st;

@@ -163,11 +163,6 @@ static int scene_upload(PbrtScene* S) {
     return PBRT_OK;
 }
 
-static inline uint32_t fbits(float f) {
-    uint32_t u;
-    std::memcpy(&u, &f, 4);
-    return u;
-}
 static inline float bitsf(uint32_t u) {
     float f;
     std::memcpy(&f, &u, 4);
