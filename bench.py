@@ -148,8 +148,13 @@ def build_workload(n_rays: int):
     return prims, lights, cam, smp, rays
 
 
-def cpu_rays_per_s(prims, rays, nthreads: int, min_seconds: float = 10.0):
-    """Whole passes over `rays` on the host until `min_seconds` have passed."""
+def cpu_baseline_leg(prims, rays, nthreads: int, min_seconds: float = 10.0, sample: int = 1 << 16):
+    """The CPU-baseline leg, the only part of the GPU arm that runs the oracle:
+    whole passes over `rays` on the host until `min_seconds` have passed, and
+    the algorithmic bytes per ray of the roofline - 32 B per node tested +
+    48 B per triangle tested + 32 B ray + 16 B hit, the tests counted by the
+    oracle's reference-order traversal of a 2^16-ray sample.
+    Returns (rays/s, seconds, passes, (bytes/ray, nodes/ray, triangles/ray))."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     ob = O.OracleBVH(prims, 4, "sah")
@@ -162,15 +167,10 @@ def cpu_rays_per_s(prims, rays, nthreads: int, min_seconds: float = 10.0):
         dt = time.perf_counter() - t0
         if dt >= min_seconds:
             break
-    return passes * len(rays) / dt, dt, passes, ob
-
-
-def algorithmic_bytes_per_ray(ob, rays, sample: int = 1 << 16):
     sub = np.ascontiguousarray(rays[:: max(1, len(rays) // sample)][:sample])
     _, cnt = ob.intersect(sub, counters=True)
-    n = len(sub)
-    nodes, tris = cnt[0] / n, cnt[1] / n
-    return 32.0 * nodes + 48.0 * tris + 32.0 + 16.0, nodes, tris
+    nodes, tris = cnt[0] / len(sub), cnt[1] / len(sub)
+    return passes * len(rays) / dt, dt, passes, (32.0 * nodes + 48.0 * tris + 32.0 + 16.0, nodes, tris)
 
 
 def build_multi_scene(n: int, threads: int = 8):
@@ -561,8 +561,7 @@ def run_ours(args):
     if rank == 0:
         peak, peak_kind = measured_peak()
         nthreads = os.cpu_count() or 1
-        cpu_rps, cpu_dt, cpu_passes, ob = cpu_rays_per_s(prims, rays, nthreads)
-        bpr, nodes_pr, tris_pr = algorithmic_bytes_per_ray(ob, rays)
+        cpu_rps, cpu_dt, cpu_passes, (bpr, nodes_pr, tris_pr) = cpu_baseline_leg(prims, rays, nthreads)
         alg_bytes = bpr * N_RAYS
         achieved = alg_bytes / (mean_ms / 1e3) / 1e9
         tr = committed_traffic()
