@@ -349,12 +349,21 @@ int pbrtgpu_render_tasks(const PbrtScene* scene, const PbrtCameraDesc* camera, c
  * memory, present on every GPU where the library's code is loaded until the
  * process exits; a frame needing more (about 220 bytes per sample with two
  * lights, e.g. 256x256 at 4 spp) is refused with PBRT_ERR_BUDGET, and
- * num_tasks is limited to 256.  The scene must have its device copy
- * (pbrtgpu_scene_create makes it when a device is present).  The first call
- * on a device looks up the scratch's device address; make that first call
- * before any stream capture.  All calls share the one scratch array: calls
- * that overlap on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  Results equal pbrtgpu_render's. */
+ * num_tasks is limited to 256; windows beyond 2^32 - 1 pixels or
+ * samples x lights are refused with PBRT_ERR_INVALID_ARGUMENT.  The scene
+ * must have its device copy (pbrtgpu_scene_create makes it when a device is
+ * present).  Set-up happens when a scene is uploaded to a device: the
+ * scratch's device address is looked up there, which also places the
+ * 64 MiB array on that device; should that fail, the first call on the
+ * device does it, so make that first call before any stream capture.  The
+ * address is looked up again after the device's context has been reset.
+ * Under CUDA's lazy module loading the render kernels' code is loaded by
+ * their first launch, as for any kernel: a caller that budgets device
+ * memory strictly makes one call (or one pbrtgpu_render) before its
+ * budgeted phase.  All calls share the one scratch array, which keeps the
+ * previous call's contents: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.  Results equal
+ * pbrtgpu_render's bit for bit. */
 int pbrtgpu_render_noalloc(const PbrtScene* scene, const PbrtCameraDesc* camera,
                            const PbrtSamplerDesc* sampler, float* rgb_out,
                            void* stream);

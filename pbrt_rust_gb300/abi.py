@@ -20,6 +20,17 @@ STATUS_NAMES = {
     4: "PBRT_ERR_UNSUPPORTED", 5: "PBRT_ERR_BUILD", 6: "PBRT_ERR_STACK_OVERFLOW", 7: "PBRT_ERR_BUDGET",
     8: "PBRT_ERR_TIMEOUT", 9: "PBRT_ERR_NAN", 10: "PBRT_ERR_NO_DEVICE", 11: "PBRT_ERR_CANCELLED",
 }
+PBRT_ERR_INVALID_ARGUMENT = 1
+PBRT_ERR_CUDA = 2
+PBRT_ERR_OUT_OF_MEMORY = 3
+PBRT_ERR_UNSUPPORTED = 4
+PBRT_ERR_BUILD = 5
+PBRT_ERR_STACK_OVERFLOW = 6
+PBRT_ERR_BUDGET = 7
+PBRT_ERR_TIMEOUT = 8
+PBRT_ERR_NAN = 9
+PBRT_ERR_NO_DEVICE = 10
+PBRT_ERR_CANCELLED = 11
 
 ABI_VERSION = 2  # PBRT_GPU_ABI_VERSION
 

@@ -290,14 +290,10 @@ __global__ void __launch_bounds__(BLOCK) kb_replay(BatchArgs A) {
 // FLAT: kb_trace_flat (the stage's refill is 32), else kb_trace.
 template <int BLOCK, bool SHADOW, bool WIDE, int S1, int S2, int MODE, bool FLAT>
 cudaError_t go(const BatchArgs& A, int sms, cudaStream_t s) {
-    static int bps = 0;
+    static ShapeCache bps_cache;
     const size_t smem = WIDE ? (size_t)S1 * sizeof(uint2) * BLOCK : 0;
     auto kernel = FLAT ? kb_trace_flat<BLOCK, SHADOW, WIDE, S1, S2, MODE> : kb_trace<BLOCK, SHADOW, WIDE, S1, S2, MODE>;
-    if (bps == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel, BLOCK, smem);
-        if (e != cudaSuccess) return e;
-        if (bps < 1) bps = 1;
-    }
+    const int bps = resident_blocks(bps_cache, kernel, BLOCK, smem);
     kernel<<<(unsigned)(sms * bps), BLOCK, smem, s>>>(A);
     return cudaGetLastError();
 }

@@ -113,4 +113,14 @@ void gather_offsets(float filter_width, int32_t sampler_start, int32_t sampler_e
 void sub_window(const PbrtSamplerDesc& s, size_t num, int32_t out[4]);
 void film_extent(uint32_t xres, uint32_t yres, const float crop[4], int32_t ext[4]);
 void chacha_key(uint64_t state, uint32_t key[8]);
+// Pixels and samples of the sampler's window, refused with
+// PBRT_ERR_INVALID_ARGUMENT when the window is empty, a side exceeds
+// INT32_MAX, or the pixels or (samples x lights) exceed the 32-bit ray and
+// shadow-queue indices (capi_render.cu).
+int sampler_counts(const PbrtSamplerDesc* smp, uint32_t spp, uint32_t n_lights, uint32_t* n_pixels,
+                   uint64_t* n_samples);
+// Resolves the no-allocation render's scratch on `dev` (the current device),
+// which loads its 64 MiB array there; called when a scene is uploaded so the
+// array is in place before any render (capi_noalloc.cu).
+int noalloc_prepare(int dev);
 }

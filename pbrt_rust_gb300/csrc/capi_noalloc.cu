@@ -11,6 +11,7 @@
 // data, the shadow-ray queue, counters, the task and filter tables and,
 // for host outputs, the staging of the image) carved out of one fixed
 // array of device memory that exists for the life of the process.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -38,23 +39,68 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kNoAllocMaxDevices = 64;
 constexpr uint32_t kNoAllocMaxTasks = 256;
 static std::mutex g_noalloc_mu;
-static unsigned char* g_noalloc_base[kNoAllocMaxDevices];
+
+// The scratch's device address on one device, and the id of the CUDA
+// context it was looked up in: a context made after cudaDeviceReset has a
+// new id and its own copy of the array, so the address is looked up again.
+struct NoAllocSlot {
+    unsigned long long ctx_id = 0;
+    unsigned char* base = nullptr;
+};
+static NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
+
+// cuCtxGetCurrent + cuCtxGetId through the runtime's driver entry points
+// (no link against libcuda): the id of the calling thread's current context,
+// unique for the life of the process; 0 when it cannot be read.
+static unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 // Device address of the scratch on `dev`, which must be the current device.
 // In host code the array's name is only a host-side stand-in, never a
 // device address, so the address comes from cudaGetSymbolAddress, looked
-// up once per device.
-static int noalloc_scratch(int dev, unsigned char** out) {
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(PBRT_ERR_UNSUPPORTED, "device index out of range");
+// up once per device (and context); the lookup loads the array's module,
+// i.e. reserves the 64 MiB on that device.  Leaves the thread's error text
+// alone; returns the CUDA error.
+static cudaError_t noalloc_scratch(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_base[dev]) {
+    NoAllocSlot& slot = g_noalloc_slot[dev];
+    const unsigned long long ctx = current_context_id();
+    if (!slot.base || ctx != slot.ctx_id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
-        g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+        if (e != cudaSuccess) return e;
+        slot.base = static_cast<unsigned char*>(p);
+        slot.ctx_id = ctx;
     }
-    *out = g_noalloc_base[dev];
-    return PBRT_OK;
+    *out = slot.base;
+    return cudaSuccess;
+}
+
+int noalloc_prepare(int dev) {
+    unsigned char* base = nullptr;
+    return noalloc_scratch(dev, &base) == cudaSuccess ? PBRT_OK : PBRT_ERR_CUDA;
 }
 
 // Carves 256-byte aligned pieces; with base == nullptr it only measures.
@@ -91,9 +137,14 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     std::lock_guard<std::mutex> lk(S->mu);
     unsigned char* base = nullptr;
     int st;
-    if ((st = noalloc_scratch(S->bvh->device, &base))) return st;
+    if (S->bvh->device < 0 || S->bvh->device >= kNoAllocMaxDevices)
+        return set_error(PBRT_ERR_UNSUPPORTED, "device index out of range");
+    if ((st = cuda_status(noalloc_scratch(S->bvh->device, &base), "cudaGetSymbolAddress"))) return st;
     cudaStream_t s = (cudaStream_t)stream_v;
     const uint32_t nl = (uint32_t)S->lights.size();
+    uint32_t n_pixels;
+    uint64_t n_samples;
+    if ((st = sampler_counts(smp, spp, nl, &n_pixels, &n_samples))) return st;
 
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
@@ -111,8 +162,8 @@ extern "C" int pbrtgpu_render_noalloc(const PbrtScene* cS, const PbrtCameraDesc*
     P.sopen = smp->shutter_open;
     P.sclose = smp->shutter_close;
     P.words_per_pixel = (P.jitter ? 5u * spp : 0u) + 4u * spp + 9u * nl * spp;
-    P.n_pixels = (uint32_t)((P.sx1 - P.sx0) * (P.sy1 - P.sy0));
-    P.n_samples = (uint64_t)P.n_pixels * spp;
+    P.n_pixels = n_pixels;
+    P.n_samples = n_samples;
     int32_t fe[4];
     film_extent(cam->x_res, cam->y_res, cam->crop_window, fe);
     P.fx0 = fe[0];

@@ -119,6 +119,27 @@ void gather_offsets(float w, int32_t s0, int32_t s1, int32_t* lo, int32_t* hi) {
     }
 }
 
+int sampler_counts(const PbrtSamplerDesc* smp, uint32_t spp, uint32_t n_lights, uint32_t* n_pixels,
+                   uint64_t* n_samples) {
+    // window sides and area in 64 bits: int32 differences and products wrap
+    const int64_t w = (int64_t)smp->x_end - (int64_t)smp->x_start;
+    const int64_t h = (int64_t)smp->y_end - (int64_t)smp->y_start;
+    if (w <= 0 || h <= 0) return set_error(PBRT_ERR_INVALID_ARGUMENT, "empty sampler window");
+    const uint64_t area = (uint64_t)w * (uint64_t)h;
+    if (w > INT32_MAX || h > INT32_MAX || area > UINT32_MAX)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "sampler window of " + std::to_string(w) + " x " +
+                                                        std::to_string(h) + " pixels exceeds 2^32 - 1 pixels");
+    const uint64_t ns = area * spp;
+    // rays, and (sample, light) slots of the shadow queue, are indexed in 32 bits
+    if (ns * (uint64_t)std::max<uint32_t>(n_lights, 1u) > UINT32_MAX)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "the frame's " + std::to_string(ns) + " samples x " +
+                                                        std::to_string(n_lights) +
+                                                        " lights exceed 2^32 - 1 ray and shadow-queue slots");
+    *n_pixels = (uint32_t)area;
+    *n_samples = ns;
+    return PBRT_OK;
+}
+
 // rand_core 0.6.4 SeedableRng::seed_from_u64 (the published PCG32 seed
 // expansion: multiplier 6364136223846793005, increment
 // 11634580027462260723, XSH-RR output, state advanced before output).
@@ -159,6 +180,13 @@ static int scene_upload(PbrtScene* S) {
         defs.push_back(InstShade{sh, S->bvh->inst_dev[k].spheres});
     }
     if ((st = up(&S->d_inst_defs, defs))) return st;
+    // the no-allocation render's scratch is set up with the scene, not in
+    // that entry point's first call; a failure here is reported by that
+    // entry point, which tries again
+    {
+        DeviceGuard g(S->bvh->device);
+        if (noalloc_prepare(S->bvh->device) != PBRT_OK) (void)cudaGetLastError();
+    }
     S->uploaded = true;
     return PBRT_OK;
 }
@@ -419,6 +447,9 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
     int st;
     if (!S->uploaded && (st = scene_upload(S))) return st;
     const uint32_t nl = (uint32_t)S->lights.size();
+    uint32_t n_pixels;
+    uint64_t n_samples;
+    if ((st = sampler_counts(smp, spp, nl, &n_pixels, &n_samples))) return st;
 
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
@@ -436,8 +467,8 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
     P.sopen = smp->shutter_open;
     P.sclose = smp->shutter_close;
     P.words_per_pixel = (P.jitter ? 5u * spp : 0u) + 4u * spp + 9u * nl * spp;
-    P.n_pixels = (uint32_t)((P.sx1 - P.sx0) * (P.sy1 - P.sy0));
-    P.n_samples = (uint64_t)P.n_pixels * spp;
+    P.n_pixels = n_pixels;
+    P.n_samples = n_samples;
     int32_t fe[4];
     film_extent(cam->x_res, cam->y_res, cam->crop_window, fe);
     P.fx0 = fe[0];

@@ -3,11 +3,46 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/pbrt_gpu.h"
 #include "trace.cuh"
 #include "trace4.cuh"
 
 namespace pbrt {
+
+// Per-device launch-shape caches, safe to fill from several host threads at
+// once: every entry is one atomic word that holds a complete, valid value
+// (>= 1) or 0 = not yet known, so a reader never sees half of a pair.
+constexpr int kShapeCacheDevices = 64;
+using ShapeCache = std::atomic<int>[kShapeCacheDevices];
+
+// SM count of the current device.
+inline int device_sms() {
+    static ShapeCache cache;  // static storage: zero-initialised
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = (dev >= 0 && dev < kShapeCacheDevices) ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
+        if (dev >= 0 && dev < kShapeCacheDevices) cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
+// Resident blocks per SM of `kernel` on the current device, cached in the
+// caller's `cache` (one per kernel and launch configuration).
+template <class Kernel>
+inline int resident_blocks(ShapeCache& cache, Kernel kernel, int block, size_t smem) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = (dev >= 0 && dev < kShapeCacheDevices) ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (v == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, block, smem) != cudaSuccess || v < 1) v = 1;
+        if (dev >= 0 && dev < kShapeCacheDevices) cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
 
 // Largest traversal stack the kernels carry for a tree of this depth, or
 // 0 if the tree is too deep for any compiled variant.

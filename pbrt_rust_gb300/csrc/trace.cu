@@ -401,15 +401,9 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
                                           uint32_t* work, uint32_t* replay) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
-    static int bps = 0, sms = 0;
-    if (bps == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_persistent<SMAX, OVF, ANY, MINB, INST>, block,
-                                                      smem);
-        if (bps < 1) bps = 1;
-    }
+    static ShapeCache bps_cache;
+    const int sms = device_sms();
+    const int bps = resident_blocks(bps_cache, k_trace4_persistent<SMAX, OVF, ANY, MINB, INST>, block, smem);
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
     uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
     if (per_warp < 32) per_warp = 32;
@@ -436,14 +430,9 @@ static cudaError_t launch_wide_spec(const DevBVH4& bvh, const float4* r4, uint32
                                     float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream, uint32_t* work) {
     const int block = 128;
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
-    static int bps = 0, sms = 0;
-    if (bps == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace4_spec<SMAX, OVF, ANY>, block, smem);
-        if (bps < 1) bps = 1;
-    }
+    static ShapeCache bps_cache;
+    const int sms = device_sms();
+    const int bps = resident_blocks(bps_cache, k_trace4_spec<SMAX, OVF, ANY>, block, smem);
     const uint64_t warps = (uint64_t)sms * bps * (block / 32);
     if (work && g_chunk && n <= 0xF0000000u) {
         const uint64_t chunks = (n + g_chunk - 1) / g_chunk;
@@ -533,17 +522,10 @@ template <int STACK, bool ANY, bool INST = false>
 static cudaError_t launch_persistent(const DevBVH& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                      float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
                                      uint32_t* replay) {
-    static int blocks_per_sm[2][2] = {{0, 0}, {0, 0}};
-    static int sms = 0;
+    static ShapeCache bps_cache;  // one per instantiation
     const int block = 128;
-    int& bps = blocks_per_sm[STACK == 256][ANY];
-    if (bps == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace_persistent<STACK, ANY, INST>, block, 0);
-        if (bps < 1) bps = 1;
-    }
+    const int sms = device_sms();
+    const int bps = resident_blocks(bps_cache, k_trace_persistent<STACK, ANY, INST>, block, 0);
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
     uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
     if (per_warp < 32) per_warp = 32;
@@ -657,14 +639,7 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
                                 work, replay);
     if (e != cudaSuccess || occluded) return e;
     // the replay pass of closest hits (one empty launch unless a ray was marked)
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms < 1) sms = 1;
-    }
-    const unsigned grid = (unsigned)(sms * 4);
+    const unsigned grid = (unsigned)(device_sms() * 4);
     const float4* r4 = reinterpret_cast<const float4*>(rays);
     float4* h4 = reinterpret_cast<float4*>(hits);
     const bool inst = bvh.insts != nullptr;
