@@ -501,6 +501,23 @@ int pbrtgpu_server_stats(PbrtServer* server, PbrtServerStats* stats);
 /* Forgets the latency record (completed requests stay waitable). */
 int pbrtgpu_server_reset_stats(PbrtServer* server);
 
+/* The sampler's random stream on the device (RNG, src/rng.rs:4-33: rand
+ * 0.8.5 StdRng = rand_chacha 0.3.1 ChaCha12, seeded by rand_core 0.6.4
+ * seed_from_u64), exposed so that it can be checked against other
+ * implementations.  pbrtgpu_chacha_blocks: keystream blocks counter ..
+ * counter + n_blocks - 1 of the ChaCha state (the four constants, key[8],
+ * the 64-bit block counter in words 12-13, the 64-bit stream id in words
+ * 14-15) after `rounds` rounds (8, 12 or 20), by the device routine the
+ * sampler uses (paired = 1: the two-block routine, n_blocks even); 16
+ * words per block into host memory `out`.  StdRng is rounds = 12,
+ * stream_id = 0.  pbrtgpu_rng_words: words [first_word, first_word +
+ * n_words) of RNG::new(seed)'s u32 stream (rng.rs:11-13) as the render
+ * kernels read them, each run of `segment` words from its own seek.  Both
+ * synchronous; at most 2^20 blocks / 2^24 words per call. */
+int pbrtgpu_chacha_blocks(const uint32_t key[8], uint64_t counter, uint64_t stream_id, uint32_t rounds,
+                          uint32_t paired, uint32_t n_blocks, uint32_t* out);
+int pbrtgpu_rng_words(uint64_t seed, uint64_t first_word, uint32_t n_words, uint32_t segment, uint32_t* out);
+
 /* The film's 16 x 16 filter table (film.rs:89-97: the filter evaluated at
  * ((i + 0.5) / 16) of its width), row-major by y; the table every render
  * entry point uses for this camera. */

@@ -476,13 +476,16 @@ void seed_key(uint64_t state, uint32_t key[8]) {
     a += b; d ^= a; d = rotl32(d, 8);                    \
     c += d; b ^= c; b = rotl32(b, 7);
 
-void chacha12_block(const uint32_t key[8], uint64_t ctr, uint32_t out[16]) {
+// One ChaCha block of `rounds` rounds (an even count: rounds / 2 double
+// rounds of four column and four diagonal quarter rounds) over the state
+// constants | key | 64-bit block counter | 64-bit stream id, plus the input.
+void chacha_block(const uint32_t key[8], uint64_t ctr, uint64_t stream, int rounds, uint32_t out[16]) {
     uint32_t s[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u,
                       key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7],
-                      (uint32_t)ctr, (uint32_t)(ctr >> 32), 0u, 0u};
+                      (uint32_t)ctr, (uint32_t)(ctr >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)};
     uint32_t x[16];
     memcpy(x, s, sizeof(s));
-    for (int r = 0; r < 6; ++r) {
+    for (int r = 0; r < rounds / 2; ++r) {
         QR(x[0], x[4], x[8], x[12]);
         QR(x[1], x[5], x[9], x[13]);
         QR(x[2], x[6], x[10], x[14]);
@@ -494,6 +497,9 @@ void chacha12_block(const uint32_t key[8], uint64_t ctr, uint32_t out[16]) {
     }
     for (int i = 0; i < 16; ++i) out[i] = x[i] + s[i];
 }
+
+// StdRng's block: 12 rounds, stream id 0.
+void chacha12_block(const uint32_t key[8], uint64_t ctr, uint32_t out[16]) { chacha_block(key, ctr, 0, 12, out); }
 
 struct RNG {
     uint32_t key[8];
@@ -2254,6 +2260,11 @@ void oracle_rng_words(uint64_t seed, uint64_t first, uint32_t n, uint32_t* out) 
         out[i] = blk[off++];
     }
 }
+void oracle_chacha_blocks(const uint32_t key[8], uint64_t counter, uint64_t stream, uint32_t rounds,
+                          uint32_t n_blocks, uint32_t* out) {
+    for (uint32_t i = 0; i < n_blocks; ++i) chacha_block(key, counter + i, stream, (int)rounds, out + 16 * (size_t)i);
+}
+void oracle_rng_key(uint64_t seed, uint32_t key[8]) { seed_key(seed, key); }
 void oracle_rng_floats(uint64_t seed, uint32_t n, float* out) {
     RNG r(seed);
     for (uint32_t i = 0; i < n; ++i) out[i] = r.random_float();

@@ -122,6 +122,14 @@ float oracle_filter_eval(int kind, float xw, float yw, float p0, float p1,
 /* RNG (src/rng.rs:11-33): the u32 word stream of RNG::new(seed) from
  * word `first`, and sequences of draws. */
 void oracle_rng_words(uint64_t seed, uint64_t first, uint32_t n, uint32_t* out);
+/* Blocks counter .. counter + n_blocks - 1 of the ChaCha keystream with
+ * `rounds` rounds (even), the key, the 64-bit block counter in state words
+ * 12-13 and the 64-bit stream id in words 14-15: 16 words per block.
+ * StdRng's blocks are rounds = 12, stream = 0. */
+void oracle_chacha_blocks(const uint32_t key[8], uint64_t counter, uint64_t stream, uint32_t rounds,
+                          uint32_t n_blocks, uint32_t* out);
+/* The ChaCha key of RNG::new(seed) (seed_from_u64's expansion). */
+void oracle_rng_key(uint64_t seed, uint32_t key[8]);
 void oracle_rng_floats(uint64_t seed, uint32_t n, float* out);
 void oracle_rng_uints(uint64_t seed, uint32_t n, uint64_t* out);
 void oracle_rng_shuffle_i64(uint64_t seed, int64_t* v, uint32_t n, uint32_t dims,

@@ -73,6 +73,8 @@ def load() -> C.CDLL:
             "oracle_filter_eval": (C.c_float, [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                                C.c_float]),
             "oracle_rng_words": (None, [C.c_uint64, C.c_uint64, C.c_uint32, _P]),
+            "oracle_chacha_blocks": (None, [_P, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _P]),
+            "oracle_rng_key": (None, [C.c_uint64, _P]),
             "oracle_rng_floats": (None, [C.c_uint64, C.c_uint32, _P]),
             "oracle_rng_uints": (None, [C.c_uint64, C.c_uint32, _P]),
             "oracle_rng_shuffle_i64": (None, [C.c_uint64, _P, C.c_uint32, C.c_uint32, C.c_uint32]),

@@ -199,6 +199,8 @@ SIGNATURES = {
                                        C.c_uint32, _P, _P]),
     "pbrtgpu_render_noalloc": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
     "pbrtgpu_film_pixel_extent": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_int32)]),
+    "pbrtgpu_chacha_blocks": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
+    "pbrtgpu_rng_words": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _P]),
     "pbrtgpu_filter_table": (C.c_int, [C.POINTER(PbrtCameraDesc), C.POINTER(C.c_float)]),
     "pbrtgpu_write_image": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_char_p]),
     "pbrtgpu_image_bytes": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P]),

@@ -520,6 +520,44 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
 
 extern "C" {
 
+int pbrtgpu_chacha_blocks(const uint32_t key[8], uint64_t counter, uint64_t stream_id, uint32_t rounds,
+                          uint32_t paired, uint32_t n_blocks, uint32_t* out) {
+    if (!key || (!out && n_blocks)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (rounds != 8 && rounds != 12 && rounds != 20)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "rounds must be 8, 12 or 20");
+    if (n_blocks > (1u << 20)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "at most 2^20 blocks per call");
+    if (paired && (n_blocks & 1u)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "the paired routine needs an even count");
+    if (!n_blocks) return PBRT_OK;
+    if (!cuda_device_present()) return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device");
+    const size_t bytes = (size_t)n_blocks * 64;
+    uint32_t* d = nullptr;
+    int st = cuda_status(cudaMalloc((void**)&d, bytes), "cudaMalloc");
+    if (!st) st = cuda_status(launch_chacha_blocks(key, counter, stream_id, rounds, paired != 0, n_blocks, d, 0),
+                              "chacha launch");
+    if (!st) st = cuda_status(cudaMemcpy(out, d, bytes, cudaMemcpyDeviceToHost), "D2H");
+    if (d) cudaFree(d);
+    return st;
+}
+
+int pbrtgpu_rng_words(uint64_t seed, uint64_t first_word, uint32_t n_words, uint32_t segment, uint32_t* out) {
+    if (!out && n_words) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (segment == 0 || segment > 4096) return set_error(PBRT_ERR_INVALID_ARGUMENT, "segment must be in [1, 4096]");
+    if (n_words > (1u << 24)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "at most 2^24 words per call");
+    if (first_word > UINT64_MAX - n_words - 64)
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "word range past the end of the stream");
+    if (!n_words) return PBRT_OK;
+    if (!cuda_device_present()) return set_error(PBRT_ERR_NO_DEVICE, "no CUDA device");
+    uint32_t key[8];
+    chacha_key(seed, key);
+    const size_t bytes = (size_t)n_words * 4;
+    uint32_t* d = nullptr;
+    int st = cuda_status(cudaMalloc((void**)&d, bytes), "cudaMalloc");
+    if (!st) st = cuda_status(launch_rng_words(key, first_word, n_words, segment, d, 0), "rng launch");
+    if (!st) st = cuda_status(cudaMemcpy(out, d, bytes, cudaMemcpyDeviceToHost), "D2H");
+    if (d) cudaFree(d);
+    return st;
+}
+
 int pbrtgpu_render_tasks(const PbrtScene* cS, const PbrtCameraDesc* cam, const PbrtSamplerDesc* smp,
                          uint32_t task_lo, uint32_t task_hi, float* rgb_out, void* stream_v) {
     PbrtScene* S = const_cast<PbrtScene*>(cS);

@@ -29,14 +29,21 @@ __device__ __forceinline__ uint32_t rotl32(uint32_t v, int c) { return __funnels
     b ^= c;                 \
     b = rotl32(b, 7);
 
-// out[k * stride] = keystream word k of block `ctr`.
-__device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride) {
+// out[k * stride] = keystream word k of block `ctr`.  DR double rounds (6:
+// ChaCha12, StdRng's cipher) and stream id `sid` (0 for StdRng) are
+// parameters only so that the same code can be checked against other
+// ChaCha implementations (pbrtgpu_chacha_blocks); the sampler uses the
+// defaults.
+template <int DR = 6>
+__device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride,
+                                               uint64_t sid = 0) {
+    const uint32_t s14 = (uint32_t)sid, s15 = (uint32_t)(sid >> 32);
     uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
     uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
     uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
-    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = 0u, x15 = 0u;
+    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = s14, x15 = s15;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
+    for (int r = 0; r < DR; ++r) {
         PBRT_QR(x0, x4, x8, x12);
         PBRT_QR(x1, x5, x9, x13);
         PBRT_QR(x2, x6, x10, x14);
@@ -60,23 +67,26 @@ __device__ __forceinline__ void chacha12_block(const uint32_t* key, uint64_t ctr
     out[11u * stride] = x11 + key[7];
     out[12u * stride] = x12 + (uint32_t)ctr;
     out[13u * stride] = x13 + (uint32_t)(ctr >> 32);
-    out[14u * stride] = x14;
-    out[15u * stride] = x15;
+    out[14u * stride] = x14 + s14;
+    out[15u * stride] = x15 + s15;
 }
 // Blocks ctr and ctr + 1 at once (two independent chains for the
 // scheduler): word k of block ctr + j at out[(16 j + k) * stride].
-__device__ __forceinline__ void chacha12_block2(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride) {
+template <int DR = 6>
+__device__ __forceinline__ void chacha12_block2(const uint32_t* key, uint64_t ctr, uint32_t* out, uint32_t stride,
+                                                uint64_t sid = 0) {
     const uint64_t c1 = ctr + 1;
+    const uint32_t s14 = (uint32_t)sid, s15 = (uint32_t)(sid >> 32);
     uint32_t x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
     uint32_t x4 = key[0], x5 = key[1], x6 = key[2], x7 = key[3];
     uint32_t x8 = key[4], x9 = key[5], x10 = key[6], x11 = key[7];
-    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = 0u, x15 = 0u;
+    uint32_t x12 = (uint32_t)ctr, x13 = (uint32_t)(ctr >> 32), x14 = s14, x15 = s15;
     uint32_t y0 = 0x61707865u, y1 = 0x3320646eu, y2 = 0x79622d32u, y3 = 0x6b206574u;
     uint32_t y4 = key[0], y5 = key[1], y6 = key[2], y7 = key[3];
     uint32_t y8 = key[4], y9 = key[5], y10 = key[6], y11 = key[7];
-    uint32_t y12 = (uint32_t)c1, y13 = (uint32_t)(c1 >> 32), y14 = 0u, y15 = 0u;
+    uint32_t y12 = (uint32_t)c1, y13 = (uint32_t)(c1 >> 32), y14 = s14, y15 = s15;
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
+    for (int r = 0; r < DR; ++r) {
         PBRT_QR(x0, x4, x8, x12);
         PBRT_QR(y0, y4, y8, y12);
         PBRT_QR(x1, x5, x9, x13);
@@ -97,11 +107,11 @@ __device__ __forceinline__ void chacha12_block2(const uint32_t* key, uint64_t ct
     const uint32_t xs[16] = {x0 + 0x61707865u, x1 + 0x3320646eu, x2 + 0x79622d32u, x3 + 0x6b206574u,
                              x4 + key[0],      x5 + key[1],      x6 + key[2],      x7 + key[3],
                              x8 + key[4],      x9 + key[5],      x10 + key[6],     x11 + key[7],
-                             x12 + (uint32_t)ctr, x13 + (uint32_t)(ctr >> 32), x14, x15};
+                             x12 + (uint32_t)ctr, x13 + (uint32_t)(ctr >> 32), x14 + s14, x15 + s15};
     const uint32_t ys[16] = {y0 + 0x61707865u, y1 + 0x3320646eu, y2 + 0x79622d32u, y3 + 0x6b206574u,
                              y4 + key[0],      y5 + key[1],      y6 + key[2],      y7 + key[3],
                              y8 + key[4],      y9 + key[5],      y10 + key[6],     y11 + key[7],
-                             y12 + (uint32_t)c1, y13 + (uint32_t)(c1 >> 32), y14, y15};
+                             y12 + (uint32_t)c1, y13 + (uint32_t)(c1 >> 32), y14 + s14, y15 + s15};
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
         out[(uint32_t)k * stride] = xs[k];

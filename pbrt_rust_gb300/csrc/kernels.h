@@ -87,6 +87,15 @@ size_t ray_order_scratch_bytes(uint32_t n);
 // bytes, 256-byte aligned) and returns it in *order; stream-ordered.
 cudaError_t build_ray_order(const PbrtRay* rays, uint32_t n, const ReorderBounds& bounds, void* scratch,
                             uint32_t** order, cudaStream_t stream);
+// The sampler's ChaCha block code on its own (render.cu): blocks ctr ..
+// ctr + n_blocks - 1 with `rounds` rounds (8, 12 or 20) and stream id sid,
+// single-block or paired routine; and words [first, first + n) of the
+// stream with key `key` through the seekable reader, one seek per `seg`
+// words.  d_out: device memory, 16 words per block / n words.
+cudaError_t launch_chacha_blocks(const uint32_t key[8], uint64_t ctr, uint64_t sid, uint32_t rounds, bool paired,
+                                 uint32_t n_blocks, uint32_t* d_out, cudaStream_t s);
+cudaError_t launch_rng_words(const uint32_t key[8], uint64_t first, uint32_t n, uint32_t seg, uint32_t* d_out,
+                             cudaStream_t s);
 // Kernel used for the coherent camera and shadow rays of a render.
 int render_trace_kernel();
 // 64 or 256 when a compiled 4-wide variant covers this stack bound, else 0.

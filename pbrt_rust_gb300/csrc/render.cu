@@ -81,8 +81,72 @@ __global__ void __launch_bounds__(128) k_film(RenderParams P) {
     film_pixel(P, idx);
 }
 
+// ------------------------------------------------------ sampler stream ---
+// The sampler's ChaCha code, run on its own so that it can be compared with
+// other implementations: thread i computes block ctr0 + i (PAIR: blocks
+// ctr0 + 2i and ctr0 + 2i + 1 with the paired routine), 16 words a block.
+struct Key8 {
+    uint32_t k[8];
+};
+template <int DR, bool PAIR>
+__global__ void __launch_bounds__(128) k_chacha_blocks(Key8 key, uint64_t ctr0, uint64_t sid, uint32_t n_blocks,
+                                                       uint32_t* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (PAIR) {
+        if (2ull * i + 1 >= n_blocks) return;
+        chacha12_block2<DR>(key.k, ctr0 + 2ull * i, out + 32ull * i, 1u, sid);
+    } else {
+        if (i >= n_blocks) return;
+        chacha12_block<DR>(key.k, ctr0 + i, out + 16ull * i, 1u, sid);
+    }
+}
+
+// Words [first, first + n) of one task's stream as generate_pixel reads
+// them: thread t seeks to word first + t * seg and reads its segment of seg
+// words (the last one shorter) with the WordStream reader.
+__global__ void __launch_bounds__(128) k_rng_words(Key8 key, uint64_t first, uint32_t n, uint32_t seg,
+                                                   uint32_t* out) {
+    __shared__ uint32_t words[32 * 128];
+    const uint64_t lo = (uint64_t)(blockIdx.x * blockDim.x + threadIdx.x) * seg;
+    if (lo >= n) return;
+    const uint64_t hi = lo + seg < n ? lo + seg : n;
+    WordStream rng;
+    rng.seek(key.k, first + lo, first + hi, words + threadIdx.x, 128u);
+    for (uint64_t w = lo; w < hi; ++w) out[w] = rng.next_u32();
+}
+
 // ------------------------------------------------------------ launchers ---
 static inline unsigned blocks_for(uint64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+cudaError_t launch_chacha_blocks(const uint32_t key[8], uint64_t ctr, uint64_t sid, uint32_t rounds, bool paired,
+                                 uint32_t n_blocks, uint32_t* d_out, cudaStream_t s) {
+    Key8 k;
+    for (int i = 0; i < 8; ++i) k.k[i] = key[i];
+    const unsigned grid = blocks_for(paired ? (n_blocks + 1) / 2 : n_blocks, 128);
+    if (!grid) return cudaSuccess;
+    if (rounds == 8)
+        paired ? k_chacha_blocks<4, true><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out)
+               : k_chacha_blocks<4, false><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out);
+    else if (rounds == 12)
+        paired ? k_chacha_blocks<6, true><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out)
+               : k_chacha_blocks<6, false><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out);
+    else if (rounds == 20)
+        paired ? k_chacha_blocks<10, true><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out)
+               : k_chacha_blocks<10, false><<<grid, 128, 0, s>>>(k, ctr, sid, n_blocks, d_out);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rng_words(const uint32_t key[8], uint64_t first, uint32_t n, uint32_t seg, uint32_t* d_out,
+                             cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (seg == 0) return cudaErrorInvalidValue;
+    Key8 k;
+    for (int i = 0; i < 8; ++i) k.k[i] = key[i];
+    k_rng_words<<<blocks_for(((uint64_t)n + seg - 1) / seg, 128), 128, 0, s>>>(k, first, n, seg, d_out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
     cudaError_t e;
