@@ -1235,7 +1235,7 @@ struct Counters {
 };
 
 bool bvh_intersect_at(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo,
-                      int32_t* inner);
+                      int32_t* inner, bool first_hit = false);
 
 // One primitive's intersect (geometric.rs:62-73): on a hit, shrinks maxt.
 // An instance (transformed.rs:35-56) traces the primitive-space ray
@@ -1279,8 +1279,11 @@ bool prim_intersect(const Refined& R, const Prim& p, Ray& ray, float* t, float* 
 // (intersection.rs:61-66), so both use this full closest-hit search.
 // *compact gets the hit's refined index in this aggregate (hit->prim is
 // its id: with instances, the first id of the instance + the inner index).
+// first_hit: stop at the first accepted primitive (the early exit an
+// any-hit walk may take, D11: the answer is the same, the work is less);
+// used only to count that work.
 bool bvh_intersect_at(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, std::vector<uint32_t>& todo,
-                      int32_t* compact) {
+                      int32_t* compact, bool first_hit) {
     *compact = -1;
     hit->prim = -1;
     hit->t = 0;
@@ -1315,6 +1318,7 @@ bool bvh_intersect_at(const OracleBVH* o, Ray& ray, PbrtHit* hit, Counters& C, s
                     hit->b1 = b1;
                     hit->b2 = b2;
                     any = true;
+                    if (first_hit) return true;
                 }
             }
         } else {
@@ -1821,8 +1825,9 @@ float oren_nayar_term(float a, float b, V3 wo, V3 wi) {
 // WhittedIntegrator::li light loop (integrator/whitted.rs:30-65) as the
 // direct-lighting Li (D1), with Lambertian f = Kd/pi when wi, wo lie on the
 // same side of ng (bsdf/mod.rs:132-149, D7), no media (D2).
+// C counts the camera ray's traversal work, Cs the shadow rays'.
 void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, float L[3], Counters& C,
-               std::vector<uint32_t>& todo, uint64_t* n_shadow) {
+               Counters& Cs, std::vector<uint32_t>& todo, uint64_t* n_shadow) {
     L[0] = L[1] = L[2] = 0.0f;
     SurfHit h;
     if (!scene_intersect(S, ray, &h, C, todo)) return;  // miss: sum of le() is 0
@@ -1867,7 +1872,7 @@ void li_direct(const SceneData& S, const Ray& ray, const float* light_samples, f
         }
         if (f[0] == 0.0f && f[1] == 0.0f && f[2] == 0.0f) continue;
         if (n_shadow) (*n_shadow)++;
-        if (scene_occluded(S, vis, C, todo)) continue;
+        if (scene_occluded(S, vis, Cs, todo)) continue;
         float ad = fabsf(dot(wi, h.nn));
         for (int c = 0; c < 3; ++c) L[c] = L[c] + ((f[c] * Li[c]) * ad) / pdf;
     }
@@ -1932,7 +1937,7 @@ void run_task(RenderCtx& R, uint32_t task, std::vector<float>* dump, uint64_t* s
     size_t nl = R.S->lights.size(), na = integrator_floats(nl);
     std::vector<float> buf, cs(5 * n), arr(na * n + 1);
     std::vector<uint32_t> todo;
-    Counters C;
+    Counters C, Cs;
     uint64_t ncam = 0, nshadow = 0;
     for (int32_t y = w[2]; y < w[3]; ++y)
         for (int32_t x = w[0]; x < w[1]; ++x) {
@@ -1942,7 +1947,7 @@ void run_task(RenderCtx& R, uint32_t task, std::vector<float>* dump, uint64_t* s
                 const float* c = &cs[5 * i];
                 Ray ray = camera_ray(R.cam, c[0], c[1], c[2], c[3]);
                 float L[3];
-                li_direct(*R.S, ray, &arr[na * i], L, C, todo, &nshadow);
+                li_direct(*R.S, ray, &arr[na * i], L, C, Cs, todo, &nshadow);
                 ncam++;
                 if (dump) {
                     for (int k = 0; k < 5; ++k) dump->push_back(c[k]);
@@ -1962,6 +1967,12 @@ void run_task(RenderCtx& R, uint32_t task, std::vector<float>* dump, uint64_t* s
     if (stats) {
         __atomic_fetch_add(&stats[0], ncam, __ATOMIC_RELAXED);
         __atomic_fetch_add(&stats[1], nshadow, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[2], C.nodes, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[3], C.tris, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[4], C.spheres, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[5], Cs.nodes, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[6], Cs.tris, __ATOMIC_RELAXED);
+        __atomic_fetch_add(&stats[7], Cs.spheres, __ATOMIC_RELAXED);
     }
 }
 
@@ -2076,6 +2087,30 @@ static int intersect_impl(const OracleBVH* o, const PbrtRay* rays, uint32_t n, P
     }
     return 0;
 }
+int oracle_count_first_hit(const OracleBVH* o, const PbrtRay* rays, uint32_t n, uint8_t* occ, uint64_t* counters,
+                           int nthreads) {
+    std::vector<Counters> cs(std::max(nthreads, 1));
+    parallel_for(n, nthreads, [&](uint32_t lo, uint32_t hi, int t) {
+        std::vector<uint32_t> todo;
+        todo.reserve(128);
+        for (uint32_t i = lo; i < hi; ++i) {
+            Ray r = to_ray(rays[i]);
+            PbrtHit h;
+            int32_t compact;
+            bool any = bvh_intersect_at(o, r, &h, cs[t], todo, &compact, true);
+            if (occ) occ[i] = any ? 1 : 0;
+        }
+    });
+    if (counters) {
+        counters[0] = counters[1] = counters[2] = 0;
+        for (auto& c : cs) {
+            counters[0] += c.nodes;
+            counters[1] += c.tris;
+            counters[2] += c.spheres;
+        }
+    }
+    return 0;
+}
 int oracle_intersect(const OracleBVH* o, const PbrtRay* rays, uint32_t n, PbrtHit* hits, uint64_t* counters,
                      int nthreads) {
     return intersect_impl(o, rays, n, hits, nullptr, counters, nthreads);
@@ -2085,18 +2120,19 @@ int oracle_intersect_p(const OracleBVH* o, const PbrtRay* rays, uint32_t n, uint
     return intersect_impl(o, rays, n, nullptr, occ, counters, nthreads);
 }
 
-int oracle_render(const PbrtSceneDesc* scene, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler,
-                  float* rgb, int nthreads, uint32_t task_lo, uint32_t task_hi, uint64_t* stats) {
-    if (!scene || !camera || !sampler || !rgb || sampler->num_tasks == 0) return PBRT_ERR_INVALID_ARGUMENT;
+struct OracleScene {
     SceneData S;
-    int st = scene_build(scene, &S);
-    if (st) return st;
+};
+
+static int render_scene(const SceneData& S, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler, float* rgb,
+                        int nthreads, uint32_t task_lo, uint32_t task_hi, uint64_t* stats) {
     RenderCtx R;
     R.S = &S;
     R.cam = camera_new(*camera);
     R.film = film_image(camera->x_res, camera->y_res, camera_filter(*camera), camera->crop_window);
     R.sd = *sampler;
-    if (stats) stats[0] = stats[1] = 0;
+    if (stats)
+        for (int k = 0; k < 8; ++k) stats[k] = 0;
     task_hi = std::min(task_hi, sampler->num_tasks);
     std::atomic<uint32_t> next(task_lo);
     auto worker = [&]() {
@@ -2113,6 +2149,33 @@ int oracle_render(const PbrtSceneDesc* scene, const PbrtCameraDesc* camera, cons
     for (auto& t : th) t.join();
     film_write(R.film, rgb, 1.0f);
     return PBRT_OK;
+}
+
+int oracle_render(const PbrtSceneDesc* scene, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler,
+                  float* rgb, int nthreads, uint32_t task_lo, uint32_t task_hi, uint64_t* stats) {
+    if (!scene || !camera || !sampler || !rgb || sampler->num_tasks == 0) return PBRT_ERR_INVALID_ARGUMENT;
+    SceneData S;
+    int st = scene_build(scene, &S);
+    if (st) return st;
+    return render_scene(S, camera, sampler, rgb, nthreads, task_lo, task_hi, stats);
+}
+
+int oracle_scene_create(const PbrtSceneDesc* scene, OracleScene** out) {
+    if (!scene || !out) return PBRT_ERR_INVALID_ARGUMENT;
+    OracleScene* o = new OracleScene();
+    int st = scene_build(scene, &o->S);
+    if (st) {
+        delete o;
+        return st;
+    }
+    *out = o;
+    return PBRT_OK;
+}
+void oracle_scene_destroy(OracleScene* o) { delete o; }
+int oracle_scene_render(const OracleScene* o, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler,
+                        float* rgb, int nthreads, uint32_t task_lo, uint32_t task_hi, uint64_t* stats) {
+    if (!o || !camera || !sampler || !rgb || sampler->num_tasks == 0) return PBRT_ERR_INVALID_ARGUMENT;
+    return render_scene(o->S, camera, sampler, rgb, nthreads, task_lo, task_hi, stats);
 }
 
 int oracle_task_samples(const PbrtSceneDesc* scene, const PbrtCameraDesc* camera, const PbrtSamplerDesc* sampler,

@@ -56,14 +56,30 @@ int oracle_intersect(const OracleBVH* bvh, const PbrtRay* rays, uint32_t n,
                      PbrtHit* hits, uint64_t* counters, int nthreads);
 int oracle_intersect_p(const OracleBVH* bvh, const PbrtRay* rays, uint32_t n,
                        uint8_t* occluded, uint64_t* counters, int nthreads);
+/* The any-hit answer with the traversal stopped at the first accepted
+ * primitive (reference order otherwise): the work an early-exit any-hit
+ * walk does, counted as above.  The answers equal oracle_intersect_p's. */
+int oracle_count_first_hit(const OracleBVH* bvh, const PbrtRay* rays, uint32_t n,
+                           uint8_t* occluded, uint64_t* counters, int nthreads);
 
 /* Full render of SamplerRenderer::render with the restated direct-light
  * integrator.  rgb: pixel extent * 3 floats.  task_lo/task_hi select a
  * range of tasks (0, num_tasks for all); pixels of other tasks stay 0.
- * stats (may be NULL): [0] camera rays, [1] shadow rays. */
+ * stats (may be NULL, else 8 words): [0] camera rays, [1] shadow rays,
+ * [2] / [3] / [4] nodes, triangles and analytic shapes tested by the camera
+ * rays' traversals, [5] / [6] / [7] the same for the shadow rays'. */
 int oracle_render(const PbrtSceneDesc* scene, const PbrtCameraDesc* camera,
                   const PbrtSamplerDesc* sampler, float* rgb, int nthreads,
                   uint32_t task_lo, uint32_t task_hi, uint64_t* stats);
+
+/* The same render over a scene built once (BVH and shading tables), so
+ * that repeated renders time the renderer alone. */
+typedef struct OracleScene OracleScene;
+int oracle_scene_create(const PbrtSceneDesc* scene, OracleScene** out);
+void oracle_scene_destroy(OracleScene* scene);
+int oracle_scene_render(const OracleScene* scene, const PbrtCameraDesc* camera,
+                        const PbrtSamplerDesc* sampler, float* rgb, int nthreads,
+                        uint32_t task_lo, uint32_t task_hi, uint64_t* stats);
 
 /* Per-sample dump of one task, in the task's order: for each pixel of the
  * task's sub-window, for each of its samples, `stride` floats:

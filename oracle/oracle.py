@@ -46,8 +46,13 @@ def load() -> C.CDLL:
             "oracle_bvh_triangle": (C.c_int, [_P, C.c_uint32, _P]),
             "oracle_intersect": (C.c_int, [_P, _P, C.c_uint32, _P, _P, C.c_int]),
             "oracle_intersect_p": (C.c_int, [_P, _P, C.c_uint32, _P, _P, C.c_int]),
+            "oracle_count_first_hit": (C.c_int, [_P, _P, C.c_uint32, _P, _P, C.c_int]),
             "oracle_render": (C.c_int, [C.POINTER(abi.PbrtSceneDesc), C.POINTER(abi.PbrtCameraDesc),
                                         C.POINTER(abi.PbrtSamplerDesc), _P, C.c_int, C.c_uint32, C.c_uint32, _P]),
+            "oracle_scene_create": (C.c_int, [C.POINTER(abi.PbrtSceneDesc), C.POINTER(_P)]),
+            "oracle_scene_destroy": (None, [_P]),
+            "oracle_scene_render": (C.c_int, [_P, C.POINTER(abi.PbrtCameraDesc), C.POINTER(abi.PbrtSamplerDesc), _P,
+                                              C.c_int, C.c_uint32, C.c_uint32, _P]),
             "oracle_task_samples": (C.c_int, [C.POINTER(abi.PbrtSceneDesc), C.POINTER(abi.PbrtCameraDesc),
                                               C.POINTER(abi.PbrtSamplerDesc), C.c_uint32, _P, C.c_uint64, _P, _P]),
             "oracle_quadratic": (C.c_int, [C.c_float, C.c_float, C.c_float, _P, _P]),
@@ -169,6 +174,17 @@ class OracleBVH:
         self.lib.oracle_intersect(self.h, _ptr(rays), n, _ptr(hits), _ptr(cnt), nthreads or default_threads())
         return (hits, cnt) if counters else hits
 
+    def first_hit_counts(self, rays: np.ndarray, nthreads: int | None = None):
+        """(answers, counters) of the any-hit walk stopped at its first
+        accepted primitive: the early-exit work; the answers equal
+        intersect_p's."""
+        rays = np.ascontiguousarray(rays)
+        n = rays.shape[0]
+        occ = np.zeros(n, dtype=np.uint8)
+        cnt = np.zeros(3, np.uint64)
+        self.lib.oracle_count_first_hit(self.h, _ptr(rays), n, _ptr(occ), _ptr(cnt), nthreads or default_threads())
+        return occ, cnt
+
     def intersect_p(self, rays: np.ndarray, nthreads: int | None = None, counters: bool = False):
         rays = np.ascontiguousarray(rays)
         n = rays.shape[0]
@@ -186,12 +202,51 @@ def render(desc: SceneDescription, camera, sampler, num_tasks: int, nthreads: in
     smp = sampler.to_abi(num_tasks)
     x0, x1, y0, y1 = camera.film.pixel_extent()
     rgb = np.zeros((y1 - y0, x1 - x0, 3), np.float32)
-    st_arr = np.zeros(2, np.uint64)
+    st_arr = np.zeros(8, np.uint64)
     st = lib.oracle_render(C.byref(desc.desc), C.byref(cam), C.byref(smp), _ptr(rgb), nthreads or default_threads(),
                            task_lo, num_tasks if task_hi is None else task_hi, _ptr(st_arr))
     if st:
         raise abi.PbrtError(st, "oracle render failed")
     return (rgb, st_arr) if stats else rgb
+
+
+class OracleScene:
+    """A scene built once by the oracle (BVH, shading tables), rendered many
+    times: render() is the same SamplerRenderer::render restatement as the
+    module-level render(), without the per-call scene build."""
+
+    def __init__(self, desc: SceneDescription):
+        self.lib = load()
+        self.desc = desc  # keeps the description's arrays alive
+        h = C.c_void_p()
+        st = self.lib.oracle_scene_create(C.byref(desc.desc), C.byref(h))
+        if st:
+            raise abi.PbrtError(st, "oracle scene build failed")
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.oracle_scene_destroy(self.h)
+        except Exception:
+            pass
+
+    def render(self, camera, sampler, num_tasks: int, nthreads: int | None = None, task_lo: int = 0,
+               task_hi: int | None = None):
+        """Returns (rgb (h, w, 3), stats): stats as oracle_render's 8 words
+        (camera rays, shadow rays, then nodes / triangles / analytic shapes
+        tested by camera rays and by shadow rays)."""
+        cam = camera.to_abi()
+        smp = sampler.to_abi(num_tasks)
+        x0, x1, y0, y1 = camera.film.pixel_extent()
+        rgb = np.zeros((y1 - y0, x1 - x0, 3), np.float32)
+        st_arr = np.zeros(8, np.uint64)
+        st = self.lib.oracle_scene_render(self.h, C.byref(cam), C.byref(smp), _ptr(rgb),
+                                          nthreads or default_threads(), task_lo,
+                                          num_tasks if task_hi is None else task_hi, _ptr(st_arr))
+        if st:
+            raise abi.PbrtError(st, "oracle render failed")
+        return rgb, st_arr
 
 
 def task_samples(desc: SceneDescription, camera, sampler, num_tasks: int, task: int) -> np.ndarray:

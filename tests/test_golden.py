@@ -32,6 +32,30 @@ def test_soup_hits_match_golden(oracle):
     assert (g["hits"][:, 0] >= 0).sum() > 100  # the set has real hits
 
 
+def test_first_hit_walk_answers_like_the_full_search(oracle):
+    """The early-exit walk the oracle counts for the any-hit roofline gives
+    the reference's intersect_p answers (D11) with less work."""
+    g = load("soup_closest.npz")
+    prims, _ = MG.soup_inputs()
+    rays = MG.as_rays(g["rays"])
+    ob = oracle.OracleBVH(prims, 4, "sah")
+    occ, cnt = ob.first_hit_counts(rays)
+    assert np.array_equal(occ, g["occluded"])
+    _, full = ob.intersect_p(rays, counters=True)
+    assert 0 < cnt[0] < full[0] and cnt[1] <= full[1]
+
+
+def test_oracle_scene_renders_like_the_one_shot_render(oracle):
+    """OracleScene (built once, rendered many times) gives oracle.render's
+    image, and counts the traversal work of camera and shadow rays."""
+    prims, lights, cam, smp = MG.sphere_inputs()[:4]
+    nt = default_num_tasks(48, 48)
+    desc = SceneDescription(prims, lights, 4, "sah")
+    img, st = oracle.OracleScene(desc).render(cam, smp, nt)
+    assert np.array_equal(img.view(np.uint32), load("render_c1_48.npz")["rgb"].view(np.uint32))
+    assert st[0] == 48 * 48 * 4 and st[1] > 0 and st[2] > st[0] and st[5] > 0
+
+
 def test_sphere_scene_hits_match_golden(oracle):
     g = load("spheres_closest.npz")
     prims = MG.sphere_inputs()[0]
