@@ -528,7 +528,8 @@ int pbrtgpu_filter_table(const PbrtCameraDesc* camera, float table[256]);
  * of linear float as the render entry points return them.  The format
  * follows the file extension: .png / .ppm get 8-bit channels
  * (255 * p^(1/2.2) + 0.5, clamped to [0, 255] and truncated, as write_img
- * computes them), .pfm the linear floats.  pbrtgpu_image_bytes gives those
+ * computes them), .pfm and .exr (OpenEXR, scanline, uncompressed, 32-bit
+ * float B/G/R channels) the linear floats.  pbrtgpu_image_bytes gives those
  * 8-bit values without writing a file. */
 int pbrtgpu_write_image(const float* rgb, uint32_t width, uint32_t height, const char* path);
 int pbrtgpu_image_bytes(const float* rgb, uint32_t width, uint32_t height, uint8_t* out);

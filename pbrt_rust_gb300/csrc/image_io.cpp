@@ -6,7 +6,7 @@
 // through the `image` crate, the format chosen by the file extension.  Here
 // the format also follows the extension: .png and .ppm get those 8-bit
 // values (PNG written with stored - uncompressed - deflate blocks, so no
-// compression library is needed); .pfm keeps the linear float RGB.  The
+// compression library is needed); .pfm and .exr keep the linear float RGB.  The
 // reference's own write_image writes into a buffer of the wrong size and
 // overwrites the colour with the splat; the RGB given here is the intended
 // value (film_pixel's output).
@@ -108,6 +108,71 @@ std::vector<uint8_t> encode_png(const std::vector<uint8_t>& rgb8, uint32_t w, ui
     return o;
 }
 
+void le32(std::vector<uint8_t>& o, uint32_t v) {
+    for (int k = 0; k < 4; ++k) o.push_back((uint8_t)(v >> (8 * k)));
+}
+void le64(std::vector<uint8_t>& o, uint64_t v) {
+    for (int k = 0; k < 8; ++k) o.push_back((uint8_t)(v >> (8 * k)));
+}
+void lef32(std::vector<uint8_t>& o, float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    le32(o, b);
+}
+// one header attribute: name, type name, byte size, value
+void exr_attr(std::vector<uint8_t>& o, const char* name, const char* type, const std::vector<uint8_t>& value) {
+    o.insert(o.end(), name, name + std::strlen(name) + 1);
+    o.insert(o.end(), type, type + std::strlen(type) + 1);
+    le32(o, (uint32_t)value.size());
+    o.insert(o.end(), value.begin(), value.end());
+}
+
+// OpenEXR (the published file layout, version 2): a single-part scanline
+// file, no compression, one scanline per block, channels B, G, R (sorted by
+// name, as the format requires) of 32-bit float, linear values as rendered.
+std::vector<uint8_t> encode_exr(const float* rgb, uint32_t w, uint32_t h) {
+    std::vector<uint8_t> o = {0x76, 0x2f, 0x31, 0x01, 2, 0, 0, 0};  // magic, version 2 (single-part scanline)
+    std::vector<uint8_t> ch;
+    for (const char* name : {"B", "G", "R"}) {
+        ch.insert(ch.end(), name, name + 2);
+        le32(ch, 2);                        // pixel type FLOAT
+        ch.insert(ch.end(), {0, 0, 0, 0});  // pLinear, reserved
+        le32(ch, 1);                        // x sampling
+        le32(ch, 1);                        // y sampling
+    }
+    ch.push_back(0);
+    exr_attr(o, "channels", "chlist", ch);
+    exr_attr(o, "compression", "compression", {0});  // NO_COMPRESSION
+    std::vector<uint8_t> box;
+    le32(box, 0);
+    le32(box, 0);
+    le32(box, w - 1);
+    le32(box, h - 1);
+    exr_attr(o, "dataWindow", "box2i", box);
+    exr_attr(o, "displayWindow", "box2i", box);
+    exr_attr(o, "lineOrder", "lineOrder", {0});  // INCREASING_Y
+    std::vector<uint8_t> one;
+    lef32(one, 1.0f);
+    exr_attr(o, "pixelAspectRatio", "float", one);
+    std::vector<uint8_t> centre;
+    lef32(centre, 0.0f);
+    lef32(centre, 0.0f);
+    exr_attr(o, "screenWindowCenter", "v2f", centre);
+    exr_attr(o, "screenWindowWidth", "float", one);
+    o.push_back(0);  // end of header
+    const uint64_t block = 8 + (uint64_t)w * 3 * 4;  // y, byte count, B row, G row, R row
+    const uint64_t first = o.size() + 8ull * h;
+    for (uint32_t y = 0; y < h; ++y) le64(o, first + (uint64_t)y * block);
+    for (uint32_t y = 0; y < h; ++y) {
+        le32(o, y);
+        le32(o, w * 3 * 4);
+        const float* row = rgb + (size_t)y * w * 3;
+        for (int c : {2, 1, 0})
+            for (uint32_t x = 0; x < w; ++x) lef32(o, row[3 * (size_t)x + c]);
+    }
+    return o;
+}
+
 bool ends_with(const std::string& s, const char* suf) {
     const size_t n = std::strlen(suf);
     if (s.size() < n) return false;
@@ -133,7 +198,9 @@ int pbrtgpu_write_image(const float* rgb, uint32_t width, uint32_t height, const
     const std::string p(path);
     std::vector<uint8_t> file;
     const size_t n = (size_t)width * height * 3;
-    if (ends_with(p, ".pfm")) {
+    if (ends_with(p, ".exr")) {
+        file = encode_exr(rgb, width, height);
+    } else if (ends_with(p, ".pfm")) {
         // Portable float map: little-endian (scale -1), rows bottom to top
         std::string hdr = "PF\n" + std::to_string(width) + " " + std::to_string(height) + "\n-1.0\n";
         file.assign(hdr.begin(), hdr.end());
@@ -155,7 +222,7 @@ int pbrtgpu_write_image(const float* rgb, uint32_t width, uint32_t height, const
             file.assign(hdr.begin(), hdr.end());
             file.insert(file.end(), rgb8.begin(), rgb8.end());
         } else {
-            return set_error(PBRT_ERR_UNSUPPORTED, "image format: use .png, .ppm or .pfm");
+            return set_error(PBRT_ERR_UNSUPPORTED, "image format: use .png, .ppm, .pfm or .exr");
         }
     }
     FILE* f = std::fopen(path, "wb");

@@ -71,6 +71,53 @@ def test_png_ppm_pfm_round_trip(lib, rgb, tmp_path):
     assert np.array_equal(back.view(np.uint32), rgb.view(np.uint32))
 
 
+def read_exr(path):
+    """A reader of the OpenEXR layout (magic, version, header attributes,
+    scanline offset table, uncompressed one-line blocks) written from the
+    published file-format description: returns (attributes, channels,
+    (h, w, 3) RGB)."""
+    import struct
+    data = open(path, "rb").read()
+    assert data[:4] == bytes([0x76, 0x2F, 0x31, 0x01]) and struct.unpack("<I", data[4:8])[0] == 2
+    pos, attrs = 8, {}
+    while data[pos] != 0:
+        end = data.index(b"\0", pos)
+        name = data[pos:end].decode()
+        tend = data.index(b"\0", end + 1)
+        typ = data[end + 1:tend].decode()
+        size = struct.unpack("<i", data[tend + 1:tend + 5])[0]
+        attrs[name] = (typ, data[tend + 5:tend + 5 + size])
+        pos = tend + 5 + size
+    pos += 1
+    chl = attrs["channels"][1]
+    chans, q = [], 0
+    while chl[q] != 0:
+        e = chl.index(b"\0", q)
+        ptype, _, xs, ys = struct.unpack("<iIii", chl[e + 1:e + 17])
+        chans.append((chl[q:e].decode(), ptype, xs, ys))
+        q = e + 17
+    x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"][1])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    offsets = struct.unpack(f"<{h}Q", data[pos:pos + 8 * h])
+    planes = {c[0]: np.zeros((h, w), np.float32) for c in chans}
+    for off in offsets:
+        y, nbytes = struct.unpack("<iI", data[off:off + 8])
+        assert nbytes == 4 * w * len(chans)
+        row = np.frombuffer(data[off + 8:off + 8 + nbytes], "<f4").reshape(len(chans), w)
+        for k, c in enumerate(chans):
+            planes[c[0]][y - y0] = row[k]
+    return attrs, chans, np.stack([planes["R"], planes["G"], planes["B"]], axis=-1)
+
+
+def test_exr_holds_the_linear_floats(lib, rgb, tmp_path):
+    write_image(rgb, tmp_path / "a.exr")
+    attrs, chans, back = read_exr(tmp_path / "a.exr")
+    assert [c[0] for c in chans] == ["B", "G", "R"] and all(c[1:] == (2, 1, 1) for c in chans)  # FLOAT
+    assert attrs["compression"] == ("compression", b"\x00") and attrs["lineOrder"] == ("lineOrder", b"\x00")
+    assert attrs["displayWindow"] == attrs["dataWindow"]
+    assert np.array_equal(back.view(np.uint32), rgb.view(np.uint32))
+
+
 def test_big_png_uses_several_deflate_blocks(lib, tmp_path):
     rgb = np.random.default_rng(1).uniform(0, 1, size=(200, 150, 3)).astype(np.float32)  # 90 kB of scanlines
     write_image(rgb, tmp_path / "b.png")
