@@ -317,6 +317,10 @@ int pbrtgpu_get_trace_config(PbrtTraceConfig* cfg);
  * pbrtgpu_bvh_create. */
 int pbrtgpu_scene_create(const PbrtSceneDesc* desc, PbrtScene** out);
 void pbrtgpu_scene_destroy(PbrtScene* scene);
+/* Device bytes a scene holds: its BVH's (pbrtgpu_bvh_device_bytes) plus its
+ * shading tables, lights and instance records; per-render scratch not
+ * included. */
+int pbrtgpu_scene_device_bytes(const PbrtScene* scene, uint64_t* bytes);
 /* The scene's aggregate, usable with pbrtgpu_intersect*. */
 int pbrtgpu_scene_bvh(const PbrtScene* scene, const PbrtBVH** out);
 
@@ -462,12 +466,22 @@ int pbrtgpu_batch_autotune(PbrtBatch* batch, void* stream, uint32_t repeats, Pbr
  * `slots` batches are in flight together (each on its own stream).  A
  * request larger than a slot's limits is refused at submission with
  * PBRT_ERR_BUDGET.  Each result equals what the single-request entry point
- * gives (bit for bit), alone or in any mix. */
+ * gives (bit for bit), alone or in any mix.
+ *
+ * Device-memory pool: with pool_bytes > 0 the server holds its resident
+ * scenes and its slots' arenas to that budget.  The slots are charged at
+ * creation (PBRT_ERR_BUDGET if they alone exceed it); a scene or BVH
+ * becomes resident by pbrtgpu_server_admit, charged its device bytes, and
+ * is refused with PBRT_ERR_BUDGET when it would not fit; requests name
+ * resident scenes (a render) or resident BVHs, a scene's own BVH included
+ * (a query), others are refused at submission.  pool_bytes = 0: no pool
+ * accounting and any scene may be named. */
 typedef struct PbrtServerConfig {
     uint32_t slots;          /* batches in flight at once, 1..8 */
     uint32_t use_tuning;     /* 1: apply `tuning` to every slot */
     PbrtBatchLimits limits;  /* device memory of each slot (pbrtgpu_batch_bytes) */
     PbrtBatchTuning tuning;
+    uint64_t pool_bytes;     /* device budget of resident scenes + slot arenas; 0 = none */
 } PbrtServerConfig;
 
 typedef struct PbrtServerStats {
@@ -476,11 +490,25 @@ typedef struct PbrtServerStats {
     double p50_ms, p99_ms, mean_ms, max_ms;  /* submission to result, completed requests */
     double span_s;                           /* first submission to last result */
     double requests_per_s;                   /* completed / span_s */
+    /* pool: budget, bytes of the slot arenas and of the resident scenes and
+     * BVHs (and how many), requests that found the free slot full and
+     * waited for the next one, requests refused (not resident, larger than
+     * a slot, invalid) */
+    uint64_t pool_bytes, slot_bytes, resident_bytes, resident_count;
+    uint64_t deferred, refused;
 } PbrtServerStats;
 
 typedef struct PbrtServer PbrtServer;
 
 int pbrtgpu_server_create(const PbrtServerConfig* config, PbrtServer** out);
+/* Makes a scene (and with it its BVH) or a bare BVH resident in the
+ * server's pool: exactly one of scene / bvh is non-NULL.  Charged its
+ * device bytes (pbrtgpu_scene_device_bytes / pbrtgpu_bvh_device_bytes);
+ * PBRT_ERR_BUDGET if the pool cannot hold it.  Admitting a resident handle
+ * again changes nothing.  pbrtgpu_server_release takes it out of the pool
+ * (its requests must have completed). */
+int pbrtgpu_server_admit(PbrtServer* server, const PbrtScene* scene, const PbrtBVH* bvh);
+int pbrtgpu_server_release(PbrtServer* server, const PbrtScene* scene, const PbrtBVH* bvh);
 /* Finishes every submitted request, then frees the server. */
 void pbrtgpu_server_destroy(PbrtServer* server);
 /* The camera and sampler descriptions are copied; the scene, rgb_out and

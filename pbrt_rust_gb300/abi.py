@@ -141,14 +141,16 @@ class PbrtBatchTuning(C.Structure):
 
 class PbrtServerConfig(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("use_tuning", C.c_uint32), ("limits", PbrtBatchLimits),
-                ("tuning", PbrtBatchTuning)]
+                ("tuning", PbrtBatchTuning), ("pool_bytes", C.c_uint64)]
 
 
 class PbrtServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("batches", C.c_uint64), ("mean_batch_requests", C.c_double), ("p50_ms", C.c_double),
                 ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
-                ("requests_per_s", C.c_double)]
+                ("requests_per_s", C.c_double), ("pool_bytes", C.c_uint64), ("slot_bytes", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("resident_count", C.c_uint64), ("deferred", C.c_uint64),
+                ("refused", C.c_uint64)]
 
 
 class PbrtBatchStats(C.Structure):
@@ -193,6 +195,7 @@ SIGNATURES = {
     "pbrtgpu_get_trace_config": (C.c_int, [C.POINTER(PbrtTraceConfig)]),
     "pbrtgpu_scene_create": (C.c_int, [C.POINTER(PbrtSceneDesc), C.POINTER(_P)]),
     "pbrtgpu_scene_destroy": (None, [_P]),
+    "pbrtgpu_scene_device_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "pbrtgpu_scene_bvh": (C.c_int, [_P, C.POINTER(_P)]),
     "pbrtgpu_render": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P, _P]),
     "pbrtgpu_render_tasks": (C.c_int, [_P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), C.c_uint32,
@@ -218,6 +221,8 @@ SIGNATURES = {
     "pbrtgpu_batch_stats": (C.c_int, [_P, C.POINTER(PbrtBatchStats)]),
     "pbrtgpu_batch_autotune": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(PbrtBatchTuning), C.POINTER(C.c_float)]),
     "pbrtgpu_server_create": (C.c_int, [C.POINTER(PbrtServerConfig), C.POINTER(C.c_void_p)]),
+    "pbrtgpu_server_admit": (C.c_int, [_P, _P, _P]),
+    "pbrtgpu_server_release": (C.c_int, [_P, _P, _P]),
     "pbrtgpu_server_destroy": (None, [_P]),
     "pbrtgpu_server_submit_render": (C.c_int, [_P, _P, C.POINTER(PbrtCameraDesc), C.POINTER(PbrtSamplerDesc), _P,
                                                C.POINTER(C.c_uint64)]),

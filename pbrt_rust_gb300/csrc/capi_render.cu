@@ -520,6 +520,19 @@ int prepare_render(PbrtScene* S, const PbrtCameraDesc* cam, const PbrtSamplerDes
 
 extern "C" {
 
+int pbrtgpu_scene_device_bytes(const PbrtScene* S, uint64_t* bytes) {
+    if (!S || !bytes) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    uint64_t n = 0;
+    int st = pbrtgpu_bvh_device_bytes(S->bvh, &n);
+    if (st) return st;
+    n += S->shade.size() * sizeof(ShadePrim) + S->materials.size() * sizeof(float4) +
+         S->lights.size() * sizeof(LightRec) + S->area_tris.size() * sizeof(AreaTri) + S->area_cdf.size() * sizeof(float) +
+         S->inst_map.size() * sizeof(uint4) + S->inst_shade.size() * sizeof(InstShade);
+    for (const auto& v : S->inst_shade) n += v.size() * sizeof(ShadePrim);
+    *bytes = n;
+    return PBRT_OK;
+}
+
 int pbrtgpu_chacha_blocks(const uint32_t key[8], uint64_t counter, uint64_t stream_id, uint32_t rounds,
                           uint32_t paired, uint32_t n_blocks, uint32_t* out) {
     if (!key || (!out && n_blocks)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");

@@ -69,8 +69,15 @@ struct PbrtServer {
     std::condition_variable cv_work, cv_done;
     std::thread worker;
     bool stop = false;
+    // device-memory pool (cfg.pool_bytes > 0): the slots' arenas and the
+    // resident handles (scene or BVH -> bytes charged; a scene's BVH is
+    // resident with it)
+    uint64_t slot_bytes = 0, resident_bytes = 0;
+    std::unordered_map<const void*, uint64_t> resident;
+    std::unordered_map<const PbrtBVH*, uint32_t> resident_bvh;  // -> handles that make it resident
     // statistics
     uint64_t submitted = 0, completed = 0, failed = 0, batches = 0, batched_requests = 0;
+    uint64_t deferred = 0, refused = 0;
     std::vector<double> latency_ms;
     bool have_first = false;
     Clock::time_point first_submit, last_done;
@@ -119,6 +126,7 @@ bool PbrtServer::fill(Slot& s) {
         if (st == PBRT_ERR_BUDGET && !take.empty()) {  // full: it waits for the next slot, still first in line
             std::lock_guard<std::mutex> lk(mu);
             pending.push_front(r);
+            ++deferred;
             break;
         }
         if (st) {  // it can never run (invalid, or larger than a whole slot)
@@ -128,6 +136,7 @@ bool PbrtServer::fill(Slot& s) {
             r->done = true;
             ++completed;
             ++failed;
+            ++refused;
             cv_done.notify_all();
             continue;
         }
@@ -219,8 +228,14 @@ int pbrtgpu_server_create(const PbrtServerConfig* cfg, PbrtServer** out) {
     if (!cfg || !out) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
     if (cfg->slots < 1 || cfg->slots > 8) return set_error(PBRT_ERR_INVALID_ARGUMENT, "slots must be in [1, 8]");
+    uint64_t per_slot = 0;
+    if (int st0 = pbrtgpu_batch_bytes(&cfg->limits, &per_slot, nullptr)) return st0;
+    if (cfg->pool_bytes && per_slot * cfg->slots > cfg->pool_bytes)
+        return set_error(PBRT_ERR_BUDGET, "the slots' arenas (" + std::to_string(per_slot * cfg->slots) +
+                                              " bytes) exceed the pool of " + std::to_string(cfg->pool_bytes));
     PbrtServer* S = new PbrtServer();
     S->cfg = *cfg;
+    S->slot_bytes = per_slot * cfg->slots;
     int st = cuda_status(cudaGetDevice(&S->device), "cudaGetDevice");
     for (uint32_t i = 0; !st && i < cfg->slots; ++i) {
         Slot s;
@@ -258,14 +273,68 @@ void pbrtgpu_server_destroy(PbrtServer* S) {
     delete S;
 }
 
+namespace {
+
+// A submission naming a handle outside the pool is refused (pool mode only).
+int check_resident(PbrtServer* S, const void* handle, bool is_bvh) {
+    if (!S->cfg.pool_bytes) return PBRT_OK;
+    std::lock_guard<std::mutex> lk(S->mu);
+    const bool ok = is_bvh ? S->resident_bvh.count(static_cast<const PbrtBVH*>(handle)) != 0
+                           : S->resident.count(handle) != 0;
+    if (ok) return PBRT_OK;
+    ++S->refused;
+    return set_error(PBRT_ERR_BUDGET, is_bvh ? "the BVH is not resident in the server's pool (pbrtgpu_server_admit)"
+                                             : "the scene is not resident in the server's pool (pbrtgpu_server_admit)");
+}
+
+}  // namespace
+
+int pbrtgpu_server_admit(PbrtServer* S, const PbrtScene* scene, const PbrtBVH* bvh) {
+    if (!S || (!scene == !bvh)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "exactly one of scene and bvh");
+    const void* h = scene ? (const void*)scene : (const void*)bvh;
+    const PbrtBVH* b = scene ? scene->bvh : bvh;
+    uint64_t bytes = 0;
+    int st = scene ? pbrtgpu_scene_device_bytes(scene, &bytes) : pbrtgpu_bvh_device_bytes(bvh, &bytes);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->resident.count(h)) return PBRT_OK;
+    const uint64_t pool = S->cfg.pool_bytes;
+    if (pool && S->slot_bytes + S->resident_bytes + bytes > pool)
+        return set_error(PBRT_ERR_BUDGET, "admitting " + std::to_string(bytes) + " bytes would exceed the pool (" +
+                                              std::to_string(S->slot_bytes + S->resident_bytes) + " of " +
+                                              std::to_string(pool) + " bytes in use)");
+    S->resident[h] = bytes;
+    S->resident_bytes += bytes;
+    ++S->resident_bvh[b];
+    return PBRT_OK;
+}
+
+int pbrtgpu_server_release(PbrtServer* S, const PbrtScene* scene, const PbrtBVH* bvh) {
+    if (!S || (!scene == !bvh)) return set_error(PBRT_ERR_INVALID_ARGUMENT, "exactly one of scene and bvh");
+    const void* h = scene ? (const void*)scene : (const void*)bvh;
+    const PbrtBVH* b = scene ? scene->bvh : bvh;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->resident.find(h);
+    if (it == S->resident.end()) return set_error(PBRT_ERR_INVALID_ARGUMENT, "not resident");
+    S->resident_bytes -= it->second;
+    S->resident.erase(it);
+    auto jt = S->resident_bvh.find(b);
+    if (jt != S->resident_bvh.end() && --jt->second == 0) S->resident_bvh.erase(jt);
+    return PBRT_OK;
+}
+
 int pbrtgpu_server_submit_render(PbrtServer* S, const PbrtScene* scene, const PbrtCameraDesc* cam,
                                  const PbrtSamplerDesc* smp, float* rgb_out, uint64_t* ticket) {
     if (!S || !scene || !cam || !smp || !rgb_out) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (int st = check_resident(S, scene, false)) return st;
     const PbrtBatchLimits& L = S->cfg.limits;
     const uint64_t spp = (uint64_t)smp->x_samples * smp->y_samples;
     const int64_t w = (int64_t)smp->x_end - smp->x_start, h = (int64_t)smp->y_end - smp->y_start;
-    if (w > 0 && h > 0 && ((uint64_t)(w * h) * spp > L.max_samples || smp->num_tasks > L.max_tasks))
+    if (w > 0 && h > 0 && ((uint64_t)(w * h) * spp > L.max_samples || smp->num_tasks > L.max_tasks)) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        ++S->refused;
         return set_error(PBRT_ERR_BUDGET, "the render needs more samples or tasks than a whole batch slot holds");
+    }
     Request* r = new Request();
     r->render = true;
     r->scene = scene;
@@ -279,6 +348,7 @@ int pbrtgpu_server_submit_query(PbrtServer* S, const PbrtBVH* bvh, const PbrtRay
                                 uint8_t* occluded, uint64_t* ticket) {
     if (!S || !bvh) return set_error(PBRT_ERR_INVALID_ARGUMENT, "NULL argument");
     if (n && (!rays || (!hits && !occluded))) return set_error(PBRT_ERR_INVALID_ARGUMENT, "rays/output is NULL");
+    if (int st = check_resident(S, bvh, true)) return st;
     Request* r = new Request();
     r->render = false;
     r->bvh = bvh;
@@ -323,6 +393,12 @@ int pbrtgpu_server_stats(PbrtServer* S, PbrtServerStats* out) {
     out->failed = S->failed;
     out->batches = S->batches;
     out->mean_batch_requests = S->batches ? (double)S->batched_requests / (double)S->batches : 0.0;
+    out->pool_bytes = S->cfg.pool_bytes;
+    out->slot_bytes = S->slot_bytes;
+    out->resident_bytes = S->resident_bytes;
+    out->resident_count = S->resident.size();
+    out->deferred = S->deferred;
+    out->refused = S->refused;
     std::vector<double> v = S->latency_ms;
     if (!v.empty()) {
         std::sort(v.begin(), v.end());
@@ -353,6 +429,8 @@ int pbrtgpu_server_reset_stats(PbrtServer* S) {
     S->failed = 0;
     S->batches = 0;
     S->batched_requests = 0;
+    S->deferred = 0;
+    S->refused = 0;
     S->have_first = false;
     return PBRT_OK;
 }

@@ -194,6 +194,12 @@ class GpuScene:
         abi.check(self._lib.pbrtgpu_scene_bvh(self._h, C.byref(b)), self._lib)
         return GpuBVHAccel(None, _handle=b, _owner=self)
 
+    def device_bytes(self) -> int:
+        """Device memory the scene keeps resident (BVH + shading tables)."""
+        v = C.c_uint64()
+        abi.check(self._lib.pbrtgpu_scene_device_bytes(self._h, C.byref(v)), self._lib)
+        return v.value
+
     def close(self) -> None:
         if self._h:
             self._lib.pbrtgpu_scene_destroy(self._h)

@@ -19,11 +19,17 @@ from .gpu import GpuBVHAccel, GpuSamplerRenderer, GpuScene, _is_torch, _ray_buff
 
 
 class GpuServer:
-    def __init__(self, slots: int = 2, tuning: dict | None = None, **limit_kw):
+    """pool_bytes > 0 holds resident scenes (``admit``) and the slots' arenas
+    to that device-memory budget; requests must then name resident scenes
+    or BVHs."""
+
+    def __init__(self, slots: int = 2, tuning: dict | None = None, pool_bytes: int = 0, **limit_kw):
         self._lib = abi.load()
+        self._resident = []
         cfg = abi.PbrtServerConfig()
         cfg.slots = slots
         cfg.limits = batch_limits(**limit_kw)
+        cfg.pool_bytes = int(pool_bytes)
         if tuning:
             cfg.use_tuning = 1
             t = abi.PbrtBatchTuning()
@@ -50,6 +56,18 @@ class GpuServer:
             self.close()
         except Exception:
             pass
+
+    def admit(self, item) -> None:
+        """Makes a GpuScene (with its BVH) or a GpuBVHAccel resident in the
+        pool; raises PbrtError(PBRT_ERR_BUDGET) when it does not fit."""
+        sc, bvh = (item._h, None) if isinstance(item, GpuScene) else (None, item._h)
+        abi.check(self._lib.pbrtgpu_server_admit(self._h, sc, bvh), self._lib)
+        self._resident.append(item)  # handles stay alive while resident
+
+    def release(self, item) -> None:
+        sc, bvh = (item._h, None) if isinstance(item, GpuScene) else (None, item._h)
+        abi.check(self._lib.pbrtgpu_server_release(self._h, sc, bvh), self._lib)
+        self._resident = [x for x in self._resident if x is not item]
 
     def submit_render(self, scene: GpuScene, renderer: GpuSamplerRenderer, out=None) -> int:
         x0, x1, y0, y1 = renderer.pixel_extent()

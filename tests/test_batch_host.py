@@ -33,3 +33,17 @@ def test_batch_needs_a_device(lib):
     h = C.c_void_p()
     assert lib.pbrtgpu_batch_create(C.byref(limits()), C.byref(h)) == 10  # PBRT_ERR_NO_DEVICE
     assert not h.value
+
+
+def test_server_pool_must_hold_its_slots(lib):
+    """A server's device-memory pool is charged its slots' arenas at creation
+    (before any device work): a pool smaller than them is refused."""
+    per_slot, _ = batch_bytes(max_jobs=8, max_samples=1 << 16)
+    cfg = abi.PbrtServerConfig()
+    cfg.slots = 2
+    cfg.limits = limits(max_jobs=8, max_samples=1 << 16)
+    cfg.pool_bytes = 2 * per_slot - 1
+    h = C.c_void_p()
+    assert lib.pbrtgpu_server_create(C.byref(cfg), C.byref(h)) == 7  # PBRT_ERR_BUDGET
+    assert b"exceed the pool" in lib.pbrtgpu_last_error()
+    assert not h.value

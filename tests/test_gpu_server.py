@@ -109,3 +109,43 @@ def test_flood_is_batched(pool):
     st = server.stats()
     assert st["mean_batch_requests"] > 1.5, st
     server.close()
+
+
+def test_pool_budget_admits_scenes_and_refuses_others(pool):
+    """With a device-memory pool the slots and the resident scenes share the
+    budget: a scene that does not fit is refused, requests may only name
+    resident scenes or their BVHs, and served results stay the ones alone."""
+    from pbrt_rust_gb300.batch import batch_bytes
+    reqs, alone, scenes = pool
+    lim = dict(max_jobs=64, max_samples=1 << 16, max_film_pixels=1 << 14, max_tasks=1 << 10)
+    slot = batch_bytes(**lim)[0]
+    sizes = [sc.device_bytes() for sc in scenes]
+    assert all(s > 0 for s in sizes)
+    budget = 2 * slot + sum(sizes[:4])  # room for four of the five scenes
+    srv = GpuServer(slots=2, pool_bytes=budget, **lim)
+    try:
+        for sc in scenes[:4]:
+            srv.admit(sc)
+        with pytest.raises(abi.PbrtError) as e:
+            srv.admit(scenes[4])
+        assert e.value.status == abi.PBRT_ERR_BUDGET
+        st = srv.stats()
+        assert st["pool_bytes"] == budget and st["slot_bytes"] == 2 * slot
+        assert st["resident_bytes"] == sum(sizes[:4]) and st["resident_count"] == 4
+        tickets = []
+        for r, want in zip(reqs, alone):
+            sc_index = next(k for k, sc in enumerate(scenes) if (r[1] is sc or getattr(r[1], "_owner", None) is sc))
+            if sc_index == 4:
+                with pytest.raises(abi.PbrtError) as e:
+                    submit(srv, r)
+                assert e.value.status == abi.PBRT_ERR_BUDGET
+            else:
+                tickets.append((submit(srv, r), want))
+        for t, want in tickets:
+            assert np.array_equal(bits(srv.wait(t)), bits(want))
+        assert srv.stats()["refused"] == 3  # the fifth scene's two renders and query
+        srv.release(scenes[0])
+        srv.admit(scenes[4])  # now it fits
+        assert srv.stats()["resident_bytes"] == sum(sizes[1:5])
+    finally:
+        srv.close()
