@@ -3,6 +3,7 @@
   python -m pbrt_rust_gb300.profile trace  [--rays N] [--any] [--repeat R]
   python -m pbrt_rust_gb300.profile render [--res R] [--spp-side S] [--repeat R]
   python -m pbrt_rust_gb300.profile batch  [--scenes N] [--repeat R]
+  python -m pbrt_rust_gb300.profile served [--scenes N] [--requests Q] [--slots K] [--repeat R]
 
 `trace` and `render` use the 708x708 heightfield scene; `trace` runs R
 closest-hit (or any-hit) passes over N incoherent rays, `render` R frames of
@@ -10,26 +11,111 @@ the direct-lighting wavefront.  `batch` renders the multi-scene workload
 (N scenes of 1k-256k triangles + 0-32 spheres, 128-512 squared, 1/4/16 spp)
 as one batch R times, with the tuning the autotuner picks for it (binary
 walks, 256 threads, refill 32: the flat traversal stages).  Each pass is
-timed with CUDA events on its stream.
+timed with CUDA events on its stream.  `served` builds the serving workload
+(N resident scenes of 10k-1M triangles, Q requests: renders 128-512 squared
+at 1/4 spp and ray batches of 2^14-2^18 rays), runs every request once
+through the one-request calls, then R floods of all Q through a server with
+K slots, and prints wall-clock requests/s of both.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes as C
 import sys
+import time
 
 import numpy as np
 
 
+def serving_pool(n_scenes: int = 32, threads: int = 8):
+    """The resident scenes of the serving workload: n_scenes random-triangle
+    soups of 10k-1M triangles (log uniform) with 0-32 spheres, two lights
+    each.  Returns [(GpuScene, GpuBVHAccel, Camera)]."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from . import generators as G
+    from .gpu import GpuScene
+
+    def one(i):
+        prims, lights, cam, _ = G.multi_scene(i, seed=G.config_seed(4, i), tri_range=(10000, 1000000),
+                                              res_choices=(128,), spp_choices=(1,))
+        sc = GpuScene(prims, lights)
+        return sc, sc.aggregate(), cam
+
+    with ThreadPoolExecutor(threads) as ex:  # host BVH builds release the GIL
+        return list(ex.map(one, range(n_scenes)))
+
+
+def serving_requests(pool, n_requests: int, device, seed: int | None = None):
+    """The request stream over `pool`: ("render", scene, renderer, out) or
+    ("query", bvh, rays, out) tuples, rays and outputs on `device`.  Ray
+    batches of the same scene and size share one ray array (each request
+    has its own output)."""
+    import torch
+
+    from . import generators as G
+    from .gpu import GpuSamplerRenderer
+    from .scene import Camera, Film, Filter, StratifiedSampler
+    reqs = []
+    ray_sets = {}
+    for spec in G.serving_requests(n_requests, len(pool), seed=seed):
+        sc, bvh, cam = pool[spec["scene"]]
+        if spec["kind"] == "render":
+            res, side = spec["res"], 1 if spec["spp"] == 1 else 2
+            film = Film.image(res, res, Filter.mean(0.5, 0.5))
+            c = G.orbit_camera(Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, 60.0,
+                                                  film), spec["radius"], spec["azimuth"])
+            smp = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
+            reqs.append(("render", sc, GpuSamplerRenderer(smp, c), torch.empty((res, res, 3), device=device)))
+        else:
+            key = (spec["scene"], spec["n"])
+            if key not in ray_sets:
+                lo, hi = bvh.world_bound()
+                rays = G.incoherent_rays(G.PCG32(spec["seed"]), spec["n"], lo, hi)
+                ray_sets[key] = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(device)
+            reqs.append(("query", bvh, ray_sets[key], torch.empty((spec["n"], 4), device=device)))
+    return reqs
+
+
+def run_plain(reqs, stream) -> None:
+    """Every request through its one-request call, each finished before the
+    next starts (renders return after the frame; queries synchronise)."""
+    for r in reqs:
+        if r[0] == "render":
+            r[2].render(r[1], out=r[3], stream=stream)
+        else:
+            r[1].intersect(r[2], out=r[3], stream=stream)
+            stream.synchronize()
+
+
+def run_served(srv, reqs, outs, arrivals=None) -> dict:
+    """Submits every request (at `arrivals` seconds from the start when
+    given, else at once), waits for all, returns the server's statistics."""
+    srv.reset_stats()
+    tickets = []
+    t0 = time.perf_counter()
+    for k, (r, o) in enumerate(zip(reqs, outs)):
+        if arrivals is not None:
+            while time.perf_counter() - t0 < arrivals[k]:
+                pass
+        tickets.append(srv.submit_render(r[1], r[2], out=o) if r[0] == "render"
+                       else srv.submit_query(r[1], r[2], out=o))
+    for t in tickets:
+        srv.wait(t)
+    return srv.stats()
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["trace", "render", "batch"])
+    ap.add_argument("what", choices=["trace", "render", "batch", "served"])
     ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--rays", type=int, default=1 << 20)
     ap.add_argument("--any", action="store_true")
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--res", type=int, default=256)
     ap.add_argument("--spp-side", type=int, default=2)
+    ap.add_argument("--requests", type=int, default=400)
+    ap.add_argument("--slots", type=int, default=2)
     a = ap.parse_args(argv)
     import torch
 
@@ -42,6 +128,25 @@ def main(argv=None) -> int:
     stream = torch.cuda.Stream()
     sh = C.c_void_p(stream.cuda_stream)
     times = []
+    if a.what == "served":
+        from .server import GpuServer
+        pool = serving_pool(min(a.scenes, 32))
+        reqs = serving_requests(pool, a.requests, torch.device("cuda"))
+        run_plain(reqs[:20], stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run_plain(reqs, stream)
+        plain_s = time.perf_counter() - t0
+        srv = GpuServer(slots=a.slots, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22,
+                        max_query_rays=1 << 20, max_tasks=1 << 14)
+        outs = [torch.empty_like(r[3]) for r in reqs]
+        for _ in range(a.repeat):
+            st = run_served(srv, reqs, outs)
+            print(f"served: {st['requests_per_s']:.0f} requests/s, {st['batches']} batches, mean "
+                  f"{st['mean_batch_requests']:.1f} requests, p50 {st['p50_ms']:.2f} ms, p99 {st['p99_ms']:.2f} ms")
+        srv.close()
+        print(f"plain: {len(reqs) / plain_s:.0f} requests/s")
+        return 0
     if a.what == "batch":
         from concurrent.futures import ThreadPoolExecutor
 
