@@ -236,120 +236,288 @@ def bench_batched(torch, dev, stream, n_scenes: int = 64):
             "kernels_per_launch": stats["kernels"], "graph": bool(stats["graph"]), "bit_exact": exact}
 
 
-def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 400, rate: float = 1000.0):
+SWEEP_RATES = (50.0, 200.0, 500.0, 1000.0, 2000.0)
+POOL_BYTES = 120 * 10**9  # the serving workload's device-memory budget
+
+
+def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000, rates=SWEEP_RATES, slots: int = 2):
     """Requests/s and latency of the serving loop against the plain path
     (one request at a time through pbrtgpu_render / pbrtgpu_intersect) on
-    the same request stream; all outputs device-resident."""
-    from concurrent.futures import ThreadPoolExecutor
-
+    the same request stream; all outputs device-resident.  The server holds
+    the resident scenes and its slots in a 120 GB device-memory pool; the
+    flood submits every request at once, the sweep submits them as Poisson
+    arrivals at each rate."""
     from pbrt_rust_gb300 import generators as G
-    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
-    from pbrt_rust_gb300.scene import Camera, Film, Filter, StratifiedSampler
+    from pbrt_rust_gb300.profile import run_plain, run_served, serving_pool, serving_requests
     from pbrt_rust_gb300.server import GpuServer
 
-    def one(i):
-        prims, lights, cam, smp = G.multi_scene(i, seed=G.config_seed(4, i), tri_range=(10000, 1000000),
-                                                res_choices=(128,), spp_choices=(1,))
-        sc = GpuScene(prims, lights)
-        return sc, sc.aggregate(), cam
-
-    with ThreadPoolExecutor(8) as ex:
-        pool = list(ex.map(one, range(n_scenes)))
-    reqs = []
-    for spec in G.serving_requests(n_requests, n_scenes):
-        sc, bvh, cam = pool[spec["scene"]]
-        if spec["kind"] == "render":
-            res, side = spec["res"], 1 if spec["spp"] == 1 else 2
-            film = Film.image(res, res, Filter.mean(0.5, 0.5))
-            c = G.orbit_camera(Camera.perspective(cam.camera_to_world, cam.screen_window, 0.0, 1.0, 0.0, 1e30, 60.0,
-                                                  film), spec["radius"], spec["azimuth"])
-            smp = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
-            reqs.append(("render", sc, GpuSamplerRenderer(smp, c), torch.empty((res, res, 3), device=dev)))
-        else:
-            lo, hi = bvh.world_bound()
-            rays = G.incoherent_rays(G.PCG32(spec["seed"]), spec["n"], lo, hi)
-            rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
-            reqs.append(("query", bvh, rd, torch.empty((spec["n"], 4), device=dev)))
-
-    def plain(r):
-        if r[0] == "render":
-            r[2].render(r[1], out=r[3], stream=stream)  # returns after the frame is done
-        else:
-            r[1].intersect(r[2], out=r[3], stream=stream)
-            stream.synchronize()
-
-    for r in reqs[:20]:
-        plain(r)
+    pool = serving_pool(n_scenes)
+    reqs = serving_requests(pool, n_requests, dev)
+    run_plain(reqs[:20], stream)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for r in reqs:
-        plain(r)
+    run_plain(reqs, stream)
     plain_s = time.perf_counter() - t0
     ref = [r[3].clone() for r in reqs]
-    srv = GpuServer(slots=2, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22, max_query_rays=1 << 20,
-                    max_tasks=1 << 14)
+    srv = GpuServer(slots=slots, pool_bytes=POOL_BYTES, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22,
+                    max_query_rays=1 << 20, max_tasks=1 << 14)
+    for sc, _, _ in pool:
+        srv.admit(sc)
     outs = [torch.empty_like(r[3]) for r in reqs]
-
-    def serve(arrivals=None):
-        srv.reset_stats()
-        tickets = []
-        t0 = time.perf_counter()
-        for k, (r, o) in enumerate(zip(reqs, outs)):
-            if arrivals is not None:
-                while time.perf_counter() - t0 < arrivals[k]:
-                    pass
-            tickets.append(srv.submit_render(r[1], r[2], out=o) if r[0] == "render"
-                           else srv.submit_query(r[1], r[2], out=o))
-        for t in tickets:
-            srv.wait(t)
-        return srv.stats()
-
-    serve()
-    flood = serve()
+    run_served(srv, reqs, outs)
+    flood = run_served(srv, reqs, outs)
     torch.cuda.synchronize(dev)
     exact = all(torch.equal(a.view(torch.int32), b.view(torch.int32)) for a, b in zip(outs, ref))
     if not exact:
         raise RuntimeError("served results differ from the one-request results")
-    poisson = serve(G.poisson_arrivals(len(reqs), rate, seed=9))
+    sweep = []
+    for k, rate in enumerate(rates):
+        st = run_served(srv, reqs, outs, G.poisson_arrivals(len(reqs), rate, seed=9 + k))
+        sweep.append({"rate": rate, "requests": st["completed"], "requests_per_s": st["requests_per_s"],
+                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                      "max_ms": st["max_ms"], "mean_batch": st["mean_batch_requests"], "deferred": st["deferred"],
+                      "refused": st["refused"]})
+    final = srv.stats()
     srv.close()
     n_render = sum(1 for r in reqs if r[0] == "render")
     return {"scenes": n_scenes, "requests": len(reqs), "renders": n_render, "queries": len(reqs) - n_render,
-            "plain_requests_per_s": len(reqs) / plain_s, "served_requests_per_s": flood["requests_per_s"],
+            "slots": slots, "plain_requests_per_s": len(reqs) / plain_s,
+            "served_requests_per_s": flood["requests_per_s"],
             "speedup": flood["requests_per_s"] * plain_s / len(reqs),
             "flood_p50_ms": flood["p50_ms"], "flood_p99_ms": flood["p99_ms"],
-            "flood_mean_batch": flood["mean_batch_requests"],
-            "poisson_rate": rate, "poisson_requests_per_s": poisson["requests_per_s"],
-            "poisson_p50_ms": poisson["p50_ms"], "poisson_p99_ms": poisson["p99_ms"],
-            "poisson_mean_batch": poisson["mean_batch_requests"], "bit_exact": exact}
+            "flood_mean_batch": flood["mean_batch_requests"], "flood_deferred": flood["deferred"],
+            "pool": {"budget_bytes": POOL_BYTES, "slot_bytes": final["slot_bytes"],
+                     "resident_bytes": final["resident_bytes"], "resident_scenes": final["resident_count"],
+                     "admitted": "all scenes; requests name resident scenes only",
+                     "deferred_means": "a request found the free slot full and waited for the next one"},
+            "sweep": sweep, "bit_exact": exact}
 
 
-def bench_rmse(torch, dev, stream):
+def timed_events(torch, stream, flush, fn, steps: int, warmup: int):
+    """CUDA-event times (ms) of `steps` calls of fn on `stream` after
+    `warmup` untimed ones, the L2 flushed (256 MiB write) before each."""
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            flush.zero_()
+            fn()
+    torch.cuda.synchronize()
+    evs = []
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def l2_copy_gbs(torch, dev, stream, mib: int = 16, reps: int = 200) -> float:
+    """Copy bandwidth within L2 measured here: a 16 MiB buffer copied to
+    another 200 times back to back (both stay L2-resident), read + write
+    bytes over the CUDA-event time.  The L2 peak the L2-resident workloads
+    are compared with."""
+    a = torch.empty(mib << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    with torch.cuda.stream(stream):
+        for _ in range(20):
+            b.copy_(a)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            b.copy_(a)
+        e1.record(stream)
+    torch.cuda.synchronize(dev)
+    return 2.0 * a.numel() * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+def bench_c0(torch, dev, stream, flush, steps: int, warmup: int):
+    """The plain ray-BVH query workload: 4096 random triangles (SAH BVH,
+    ~0.5 MB, L2-resident) and 2^20 rays toward the centre, closest and any
+    hit, device-resident buffers, L2 flushed before each step."""
+    from pbrt_rust_gb300 import abi, generators as G
+    from pbrt_rust_gb300.gpu import GpuBVHAccel
+    lib = abi.load()
+    prims, rays = G.ray_soup(4096, 1 << 20)
+    n = len(rays)
+    bvh = GpuBVHAccel(prims, 4, "sah")
+    sh = C.c_void_p(stream.cuda_stream)
+    rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    hd = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    od = torch.empty((n,), dtype=torch.uint8, device=dev)
+    rp, hp, op = C.c_void_p(rd.data_ptr()), C.c_void_p(hd.data_ptr()), C.c_void_p(od.data_ptr())
+    ms_c = timed_events(torch, stream, flush, lambda: abi.check(lib.pbrtgpu_intersect(bvh._h, rp, n, hp, sh), lib),
+                        steps, warmup)
+    ms_a = timed_events(torch, stream, flush, lambda: abi.check(lib.pbrtgpu_intersect_p(bvh._h, rp, n, op, sh), lib),
+                        steps, warmup)
+    out = {"workload": "4096 random triangles (SAH, 1-prim leaves) + 2^20 rays toward the centre",
+           "rays": n, "closest": {"ms": statistics.mean(ms_c), "mrays_s": n / statistics.mean(ms_c) / 1e3},
+           "any": {"ms": statistics.mean(ms_a), "mrays_s": n / statistics.mean(ms_a) / 1e3},
+           "bvh_device_bytes": bvh.device_bytes(), "l2": "flushed before each step (256 MiB write)"}
+    return out, (prims, rays)
+
+
+def bench_render(torch, dev, stream, flush, prims, lights, cam, smp, frames: int = 5):
+    """Frames of the direct-lighting wavefront through pbrtgpu_render
+    (device output): CUDA-event time on the stream and wall time of the
+    call (which returns once the frame is done), L2 flushed before each."""
+    from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
+    scene = GpuScene(prims, lights)
+    r = GpuSamplerRenderer(smp, cam)
+    x0, x1, y0, y1 = cam.film.pixel_extent()
+    img = torch.empty((y1 - y0, x1 - x0, 3), dtype=torch.float32, device=dev)
+    r.render(scene, out=img, stream=stream)
+    ev, wall = [], []
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record(stream)
+        r.render(scene, out=img, stream=stream)
+        b.record(stream)
+        wall.append(time.perf_counter() - t0)
+        torch.cuda.synchronize(dev)
+        ev.append(a.elapsed_time(b))
+    spp = smp.x_samples * smp.y_samples
+    samples = (x1 - x0) * (y1 - y0) * spp
+    ms = statistics.mean(ev)
+    return {"ms_mean": ms, "ms_min": min(ev), "wall_ms_mean": 1e3 * statistics.mean(wall),
+            "images_per_s": 1e3 / ms, "samples_per_s": samples / (ms / 1e3), "samples": samples, "spp": spp,
+            "camera_rays": samples, "l2": "flushed before each frame"}, img
+
+
+def render_bytes(stats, samples: int) -> float:
+    """Algorithmic bytes of a frame from the oracle's counts of the same
+    frame (camera rays, shadow rays, then nodes / triangles / analytic
+    shapes tested by camera rays and by shadow rays): per camera ray 32 B
+    ray + 16 B hit + 32 B per node + 48 B per triangle + 16 B per analytic
+    shape tested, 16 B of material and 16 B of film per sample; per shadow
+    ray 32 B ray + 1 B answer + its nodes, triangles and shapes."""
+    cam, shadow, cn, ct, cs, sn, stt, ss = (float(x) for x in stats[:8])
+    return (cam * (32 + 16) + 32 * cn + 48 * ct + 16 * cs + samples * (16 + 16)
+            + shadow * (32 + 1) + 32 * sn + 48 * stt + 16 * ss)
+
+
+def cpu_render_leg(prims, lights, cam, smp, num_tasks: int, nthreads: int, single_tasks, min_seconds: float = 3.0):
+    """The oracle renderer (SamplerRenderer::render restated, the reference's
+    task split and per-task sub-films, one std::thread worker per host
+    thread taking whole tasks) on the same frame: whole frames with every
+    host thread until min_seconds have passed, and the tasks
+    `single_tasks` on one thread.  The scene is built once, untimed.
+    Returns (frames/s, samples/s all threads, samples/s one thread,
+    seconds, frames, single-thread samples and seconds, the oracle's work
+    counts of one frame)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from pbrt_rust_gb300.scene import SceneDescription
+    sc = O.OracleScene(SceneDescription(prims, lights))
+    x0, x1, y0, y1 = cam.film.pixel_extent()
+    spp = smp.x_samples * smp.y_samples
+    frame_samples = (x1 - x0) * (y1 - y0) * spp
+    frames, t0 = 0, time.perf_counter()
+    stats = None
+    while True:
+        _, st = sc.render(cam, smp, num_tasks, nthreads=nthreads)
+        stats = st if stats is None else stats
+        frames += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    one_samples, t1 = 0, time.perf_counter()
+    for t in single_tasks:
+        _, st = sc.render(cam, smp, num_tasks, nthreads=1, task_lo=t, task_hi=t + 1)
+        one_samples += int(st[0])
+    one_dt = time.perf_counter() - t1
+    return (frames / dt, frames * frame_samples / dt, one_samples / one_dt, dt, frames, one_samples, one_dt, stats)
+
+
+def render_report(gpu: dict, cpu, num_tasks: int, nthreads: int, single_tasks, peak: float, l2_gbs: float) -> dict:
+    fps, sps, sps1, dt, frames, one_samples, one_dt, stats = cpu
+    alg = render_bytes(stats, gpu["samples"])
+    achieved = alg / (gpu["ms_mean"] / 1e3) / 1e9
+    out = dict(gpu)
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "l2_peak": l2_gbs, "l2_frac": achieved / l2_gbs, "algorithmic_bytes_per_frame": alg,
+                       "algorithmic_bytes_per_sample": alg / gpu["samples"],
+                       "counts": {"camera_rays": int(stats[0]), "shadow_rays": int(stats[1]),
+                                  "camera_nodes": int(stats[2]), "camera_tris": int(stats[3]),
+                                  "camera_shapes": int(stats[4]), "shadow_nodes": int(stats[5]),
+                                  "shadow_tris": int(stats[6]), "shadow_shapes": int(stats[7])},
+                       "how": "oracle counts of this frame in the reference traversal order; 32 B/node, 48 B/"
+                              "triangle, 16 B/shape, rays, hits, 16 B material + 16 B film per sample"}
+    out["cpu_baseline"] = {"images_per_s": fps, "samples_per_s": sps, "unit": "images/s", "value": fps,
+                           "cores": nthreads, "hardware_concurrency": os.cpu_count(), "num_tasks": num_tasks,
+                           "kind": "port", "sample": f"{frames} whole frames in {dt:.1f} s, all host threads "
+                           f"(the reference's {num_tasks}-task split bounds the parallelism)",
+                           "single_thread": {"samples_per_s": sps1, "images_per_s": sps1 / gpu["samples"],
+                                             "cores": 1, "sample": f"tasks {list(single_tasks)} of {num_tasks}: "
+                                             f"{one_samples} samples in {one_dt:.1f} s"}}
+    return out
+
+
+# single-thread CPU samples: every third task of the frame's task split
+C2_SINGLE_TASKS = (2, 5, 8, 11)   # of the 12 tasks of 1024 x 1024
+C1_SINGLE_TASKS = (1, 4, 7)       # of the 10 tasks of 512 x 512
+
+
+def c0_report(c0: dict, data, nthreads: int, peak: float, l2_gbs: float, min_seconds: float = 3.0) -> dict:
+    """Rooflines and CPU baseline of the plain query workload: algorithmic
+    bytes per ray counted by the oracle's reference-order traversal of all
+    2^20 rays (32 B per node, 48 B per triangle, 32 B ray, 16 B hit or 1 B
+    answer; any hit counted to its first accepted primitive, as the device
+    walks it) over the CUDA-event time, against the measured HBM copy
+    bandwidth and the L2 copy bandwidth measured in this run (the BVH is
+    L2-resident); the oracle's whole passes over the rays on every host
+    thread for the CPU figure."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    prims, rays = data
+    ob = O.OracleBVH(prims, 4, "sah")
+    rays = np.ascontiguousarray(rays)
+    n = len(rays)
+    _, cnt = ob.intersect(rays, counters=True, nthreads=nthreads)
+    _, cnt_any = ob.first_hit_counts(rays, nthreads=nthreads)
+    out = dict(c0)
+    for key, k, res_bytes in (("closest", cnt, 16.0), ("any", cnt_any, 1.0)):
+        bpr = (32.0 * k[0] + 48.0 * k[1] + 16.0 * k[2]) / n + 32.0 + res_bytes
+        ach = bpr * n / (c0[key]["ms"] / 1e3) / 1e9
+        out[key]["roofline"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                                "l2_peak": l2_gbs, "l2_frac": ach / l2_gbs, "algorithmic_bytes_per_ray": bpr,
+                                "nodes_tested_per_ray": float(k[0]) / n, "tris_tested_per_ray": float(k[1]) / n}
+    passes, t0 = 0, time.perf_counter()
+    while True:
+        ob.intersect(rays, nthreads=nthreads)
+        passes += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    out["cpu_baseline"] = {"value": passes * n / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+                           "sample": f"{passes} closest-hit passes over the 2^20 rays, {dt:.1f} s"}
+    return out
+
+
+def bench_rmse(torch, dev, stream, flush):
     """The plain render config (512x512, 2x2 strata, ground, 64 spheres,
-    point + area light): frame time and RMSE (linear RGB) against the same
-    scene at 8x8 strata (64 spp, the most a pixel takes; same task split, so
-    the same task seams), whose own noise adds about 3 % to the figure.  The
-    batched and served forms produce bit-identical images, hence the same
-    RMSE."""
+    point + area light): frame time (bench_render) and RMSE (linear RGB)
+    against the same scene at 8x8 strata (64 spp, the most a pixel takes;
+    same task split, so the same task seams), whose own noise adds about 3 %
+    to the figure.  The batched and served forms produce bit-identical
+    images, hence the same RMSE."""
     from pbrt_rust_gb300 import generators as G
     from pbrt_rust_gb300.gpu import GpuSamplerRenderer, GpuScene
     prims, lights, cam, smp = G.c1_scene(res=512)
-    scene = GpuScene(prims, lights)
-    img = torch.empty((512, 512, 3), dtype=torch.float32, device=dev)
-    r4 = GpuSamplerRenderer(smp, cam)
-    r4.render(scene, out=img, stream=stream)
-    t = []
-    for _ in range(5):
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        r4.render(scene, out=img, stream=stream)
-        t.append(time.perf_counter() - t0)
+    out, img = bench_render(torch, dev, stream, flush, prims, lights, cam, smp, frames=10)
     _, _, _, smp64 = G.c1_scene(res=512, spp_side=8)
     ref = torch.empty_like(img)
-    GpuSamplerRenderer(smp64, cam).render(scene, out=ref, stream=stream)
+    GpuSamplerRenderer(smp64, cam).render(GpuScene(prims, lights), out=ref, stream=stream)
     torch.cuda.synchronize(dev)
-    rmse = float(torch.sqrt(torch.mean((img - ref) ** 2)).item())
-    return {"ms_mean": 1e3 * statistics.mean(t), "ms_min": 1e3 * min(t), "spp": 4, "rmse_vs_64spp": rmse,
-            "reference_mean": float(ref.mean().item())}
+    out["rmse_vs_64spp"] = float(torch.sqrt(torch.mean((img - ref) ** 2)).item())
+    out["reference_mean"] = float(ref.mean().item())
+    return out, (prims, lights, cam, smp)
 
 
 def bench_instanced(torch, dev, stream, n_instances: int = 256, tris_per_tree: int = 20000,
@@ -514,8 +682,11 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     hits_want = hits_dev.cpu().view(torch.int32)
 
-    def e2e_pass(mapped: bool) -> float:
-        os.environ["PBRT_HOST_MAPPED"] = "1" if mapped else "0"
+    def e2e_pass(mapped) -> float:  # None: the library's default form
+        if mapped is None:
+            os.environ.pop("PBRT_HOST_MAPPED", None)
+        else:
+            os.environ["PBRT_HOST_MAPPED"] = "1" if mapped else "0"
         for _ in range(args.warmup):
             abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
         t = []
@@ -529,25 +700,23 @@ def run_ours(args):
         hits_host.zero_()
         return N_RAYS / statistics.mean(t) / 1e6
 
-    e2e_staged = e2e_pass(False)
-    e2e_mrays = e2e_pass(True)
+    # the default and the two host-buffer forms alternate over a few rounds
+    runs = {"default": [], "staged": [], "in_place": []}
+    for _ in range(4):
+        runs["default"].append(e2e_pass(None))
+        runs["staged"].append(e2e_pass(False))
+        runs["in_place"].append(e2e_pass(True))
+    e2e_mrays = statistics.median(runs["default"])
     os.environ.pop("PBRT_HOST_MAPPED", None)
 
     # render of the same scene: 1024x1024, 16 spp, direct lighting
-    scene = GpuScene(prims, lights)
-    renderer = GpuSamplerRenderer(smp, cam)
-    img = torch.empty((1024, 1024, 3), dtype=torch.float32, device=dev)
-    renderer.render(scene, out=img, stream=stream)
-    rt = []
-    for _ in range(3):
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        renderer.render(scene, out=img, stream=stream)
-        rt.append(time.perf_counter() - t0)
+    c2, _ = bench_render(torch, dev, stream, flush, prims, lights, cam, smp, frames=5)
+    c1, c1_scene = bench_rmse(torch, dev, stream, flush)
+    c0, c0_data = bench_c0(torch, dev, stream, flush, args.steps, args.warmup)
+    l2_gbs = l2_copy_gbs(torch, dev, stream)
     instanced = bench_instanced(torch, dev, stream)
-    c1 = bench_rmse(torch, dev, stream)
     batched = bench_batched(torch, dev, stream) if not args.skip_multi else None
-    served = bench_served(torch, dev, stream) if not args.skip_multi else None
+    served = bench_served(torch, dev, stream, n_requests=args.requests) if not args.skip_multi else None
     clk.__exit__(None, None, None)
 
     mean_ms = statistics.mean(ms_closest)
@@ -562,6 +731,11 @@ def run_ours(args):
         peak, peak_kind = measured_peak()
         nthreads = os.cpu_count() or 1
         cpu_rps, cpu_dt, cpu_passes, (bpr, nodes_pr, tris_pr) = cpu_baseline_leg(prims, rays, nthreads)
+        from pbrt_rust_gb300.scene import default_num_tasks
+        nt_c2 = default_num_tasks(1024, 1024)
+        cpu_c2 = cpu_render_leg(prims, lights, cam, smp, nt_c2, nthreads, C2_SINGLE_TASKS)
+        nt_c1 = default_num_tasks(512, 512)
+        cpu_c1 = cpu_render_leg(*c1_scene, nt_c1, nthreads, C1_SINGLE_TASKS)
         alg_bytes = bpr * N_RAYS
         achieved = alg_bytes / (mean_ms / 1e3) / 1e9
         tr = committed_traffic()
@@ -580,16 +754,23 @@ def run_ours(args):
             "cpu_baseline": {"value": cpu_rps / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
                              "sample": f"{cpu_passes} passes over the 2^22 rays, {cpu_dt:.1f} s"},
             "e2e": {"value": e2e_mrays, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
-                    "d2h_bytes_per_step": N_RAYS * 16, "host_buffers": "pinned, read and written in place",
-                    "staged": {"value": e2e_staged, "unit": "Mrays/s",
-                               "how": "PBRT_HOST_MAPPED=0: H2D copy, traversal, D2H copy in 4 overlapped pieces"}},
+                    "d2h_bytes_per_step": N_RAYS * 16,
+                    "how": "median of 4 rounds of the library's default form, pinned host buffers",
+                    "forms": {k: {"median": statistics.median(v), "min": min(v), "max": max(v), "runs": v}
+                              for k, v in runs.items()},
+                    "form_meaning": {"in_place": "PBRT_HOST_MAPPED=1: the traversal reads the rays from and "
+                                                 "writes the hits to the mapped host memory",
+                                     "staged": "PBRT_HOST_MAPPED=0: H2D copy, traversal, D2H copy in 4 "
+                                               "overlapped pieces"}},
             # per timed step: the traversal kernel and the replay check (D24)
             "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),
             "any_hit": {"value": N_RAYS / (statistics.mean(ms_any) / 1e3) / 1e6, "unit": "Mrays/s"},
-            "render_1024x1024_16spp": {"ms_mean": 1e3 * statistics.mean(rt), "ms_min": 1e3 * min(rt),
-                                       "camera_rays": 1024 * 1024 * 16},
-            "render_c1_512x512_4spp": c1,
+            "render_1024x1024_16spp": render_report(c2, cpu_c2, nt_c2, nthreads, C2_SINGLE_TASKS, peak, l2_gbs),
+            "render_c1_512x512_4spp": render_report(c1, cpu_c1, nt_c1, nthreads, C1_SINGLE_TASKS, peak, l2_gbs),
+            "c0_soup_4096_tris_2e20_rays": c0_report(c0, c0_data, nthreads, peak, l2_gbs),
+            "l2_copy_gbs": {"value": l2_gbs, "how": "16 MiB buffer copied 200 times within L2, read + write bytes, "
+                                                    "CUDA events (measured in this run)"},
             "bvh_build": {"host_s": build_s, "device_s": dbuild_s, "identical": same_tree,
                           "what": "pbrtgpu_bvh_create(_ex) of the 1M-triangle heightfield, host vs device tree build"},
             "instancing": instanced,
@@ -610,9 +791,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-multi", action="store_true", help="skip the batched and served sections")
+    ap.add_argument("--requests", type=int, default=2000, help="requests of the served section (flood and each rate)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch under torch.distributed.run (what a
+        # torchrun launch does), each rank tracing its own rays against a
+        # replicated BVH; rank 0 prints the line
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()),
+               *sys.argv[1:]]
+        return subprocess.call(cmd)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
