@@ -281,16 +281,19 @@ int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
 /* Traversal kernel choice (process-wide), set by the autotuner.  Every
  * kernel visits the reference's tree in the reference's order, so results
  * do not depend on the choice.  The first value is also read from the
- * environment (PBRT_TRACE_KERNEL = plain | pt | w4 | w4pt | w4spec,
+ * environment (PBRT_TRACE_KERNEL = plain | pt | w4 | w4pt | w4spec | packet,
  * PBRT_TRACE_REFILL = 1..32, PBRT_TRACE_MINB = 0 | 8 | 9,
- * PBRT_RENDER_KERNEL = plain | w4, PBRT_TRACE_REORDER = 0 | 1,
+ * PBRT_RENDER_KERNEL = plain | w4 | packet, PBRT_TRACE_REORDER = 0 | 1,
  * PBRT_TRACE_CHUNK = 0 | 32..4096) when no call has set it. */
 enum {
     PBRT_TRACE_PAIR = 0,            /* binary pairs, one thread per ray */
     PBRT_TRACE_PAIR_PERSISTENT = 1, /* binary pairs, persistent warps */
     PBRT_TRACE_WIDE = 2,            /* 4-wide nodes, one thread per ray */
     PBRT_TRACE_WIDE_PERSISTENT = 3, /* 4-wide nodes, persistent warps */
-    PBRT_TRACE_WIDE_SPECULATIVE = 4 /* 4-wide nodes, persistent warps, leaves tested in warp-wide rounds */
+    PBRT_TRACE_WIDE_SPECULATIVE = 4, /* 4-wide nodes, persistent warps, leaves tested in warp-wide rounds */
+    PBRT_TRACE_PAIR_PACKET = 5       /* binary pairs, one thread per ray; a warp whose rays share their
+                                        direction signs walks them together, node by node, each lane
+                                        testing what its own walk tests (coherent rays) */
 };
 typedef struct PbrtTraceConfig {
     int32_t kernel;         /* PBRT_TRACE_*: pbrtgpu_intersect / intersect_p batches */

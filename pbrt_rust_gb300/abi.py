@@ -121,7 +121,7 @@ class PbrtTraceConfig(C.Structure):
                 ("render_kernel", C.c_int32), ("reorder", C.c_uint32), ("chunk", C.c_uint32)]
 
 
-TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3, "w4spec": 4}
+TRACE_KERNELS = {"plain": 0, "pt": 1, "w4": 2, "w4pt": 3, "w4spec": 4, "packet": 5}
 FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "mitchell": 3, "lanczos": 4}
 
 

@@ -50,6 +50,27 @@ __global__ void __launch_bounds__(128) k_shadow(RenderParams P) {
     P.occluded[P.shadow_slot[q]] = occ ? 1 : 0;
 }
 
+// k_shadow with warps of shadow rays that share their direction signs
+// walked together (traverse_packet); the same answers.
+template <int STACK>
+__global__ void __launch_bounds__(128) k_shadow_packet(RenderParams P) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = q < *(volatile uint32_t*)&P.counters[0];  // every lane stays for the warp's votes
+    const float4* r4 = reinterpret_cast<const float4*>(P.shadow_rays);
+    DRay r = make_dray(active ? r4[2 * (size_t)q] : make_float4(0, 0, 0, 0),
+                       active ? r4[2 * (size_t)q + 1] : make_float4(0, 0, 1, 0));
+    TraceResult res;
+    int st = 0;
+    bool occ = false;
+    if (warp_signs_uniform(r, active))
+        occ = traverse_packet<STACK, true>(P.bvh, r, active, &res, &st);
+    else if (active)
+        occ = traverse<STACK, true>(P.bvh, r, &res, &st);
+    if (!active) return;
+    if (st) atomicMax((int*)&P.counters[2], st);
+    P.occluded[P.shadow_slot[q]] = occ ? 1 : 0;
+}
+
 template <int SMAX, int OVF, bool INST = false>
 __global__ void __launch_bounds__(128) k_shadow4(RenderParams P) {
     extern __shared__ uint2 smem_stack[];
@@ -181,6 +202,10 @@ cudaError_t launch_render(const RenderParams& P, cudaStream_t s) {
                 k_shadow<64, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
             else if (inst)
                 k_shadow<256, true><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
+            else if (rk == PBRT_TRACE_PAIR_PACKET && trace_stack_for_depth(P.depth) == 64)
+                k_shadow_packet<64><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
+            else if (rk == PBRT_TRACE_PAIR_PACKET)
+                k_shadow_packet<256><<<blocks_for(max_shadow, 128), 128, 0, s>>>(P);
             else if (wv == 64)
                 k_shadow4<16, 48><<<blocks_for(max_shadow, 128), 128, smem, s>>>(P);
             else if (wv == 256)

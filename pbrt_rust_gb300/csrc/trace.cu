@@ -39,6 +39,39 @@ __global__ void __launch_bounds__(128) k_trace(const __grid_constant__ DevBVH bv
     }
 }
 
+// One thread per ray; a warp whose rays share their direction signs walks
+// them together (traverse_packet), any other warp walks each lane's ray on
+// its own (traverse).  Results equal k_trace's bit for bit.
+template <int STACK, bool ANY>
+__global__ void __launch_bounds__(128) k_trace_packet(const __grid_constant__ DevBVH bvh,
+                                                      const float4* __restrict__ rays, uint32_t n,
+                                                      const uint32_t* __restrict__ order, float4* __restrict__ hits,
+                                                      uint8_t* __restrict__ occ, int* __restrict__ status,
+                                                      uint32_t* __restrict__ replay) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;  // every lane stays for the warp's votes
+    if (active && order) i = __ldg(order + i);
+    DRay r = make_dray(active ? __ldg(rays + 2 * (size_t)i) : make_float4(0, 0, 0, 0),
+                       active ? __ldg(rays + 2 * (size_t)i + 1) : make_float4(0, 0, 1, 0));
+    TraceResult res;
+    int st = 0;
+    bool nan_hit = false, found = false;
+    if (warp_signs_uniform(r, active))
+        found = traverse_packet<STACK, ANY>(bvh, r, active, &res, &st, &nan_hit);
+    else if (active)
+        found = traverse<STACK, ANY>(bvh, r, &res, &st, &nan_hit);
+    if (!active) return;
+    if (st) atomicMax(status, st);
+    if (ANY) {
+        occ[i] = found ? 1 : 0;
+    } else if (nan_hit) {
+        hits[i] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+        *replay = 1u;
+    } else {
+        hits[i] = make_float4(__int_as_float(res.prim), res.t, res.b1, res.b2);
+    }
+}
+
 // Persistent warps: the grid holds exactly the resident warps; each warp
 // owns a contiguous range of rays and, whenever at least REFILL of its
 // lanes are idle, hands them the next rays of its range.  Rays of very
@@ -313,7 +346,8 @@ enum {
     kVariantPairPersistent = 1,
     kVariantWidePlain = 2,
     kVariantWidePersistent = 3,
-    kVariantWideSpeculative = 4
+    kVariantWideSpeculative = 4,
+    kVariantPairPacket = 5
 };
 static int g_kernel_variant = -1;
 static unsigned g_refill = 4;
@@ -328,6 +362,7 @@ static int variant_from_name(const char* v, int dflt) {
     if (!strcmp(v, "w4")) return kVariantWidePlain;
     if (!strcmp(v, "w4pt")) return kVariantWidePersistent;
     if (!strcmp(v, "w4spec")) return kVariantWideSpeculative;
+    if (!strcmp(v, "packet")) return kVariantPairPacket;
     return dflt;
 }
 
@@ -352,7 +387,7 @@ static void read_variant() {
     }
     if (const char* v = getenv("PBRT_RENDER_KERNEL")) {
         int k = variant_from_name(v, g_render_kernel);
-        if (k >= kVariantPairPlain && k <= kVariantWideSpeculative) g_render_kernel = k;
+        if (k >= kVariantPairPlain && k <= kVariantPairPacket) g_render_kernel = k;
     }
 }
 
@@ -476,9 +511,9 @@ static cudaError_t launch_wide(const DevBVH4& bvh, const float4* r4, uint32_t n,
 }
 
 int set_trace_config(const PbrtTraceConfig& c) {
-    if (c.kernel < kVariantPairPlain || c.kernel > kVariantWideSpeculative || c.refill < 1 || c.refill > 32) return 1;
+    if (c.kernel < kVariantPairPlain || c.kernel > kVariantPairPacket || c.refill < 1 || c.refill > 32) return 1;
     if (!(c.min_blocks == 0 || c.min_blocks == 7 || c.min_blocks == 8 || c.min_blocks == 9)) return 1;
-    if (c.render_kernel < kVariantPairPlain || c.render_kernel > kVariantWideSpeculative) return 1;
+    if (c.render_kernel < kVariantPairPlain || c.render_kernel > kVariantPairPacket) return 1;
     if (c.reorder > 1) return 1;
     if (!(c.chunk == 0 || (c.chunk >= 32 && c.chunk <= 4096 && c.chunk % 32 == 0))) return 1;
     read_variant();
@@ -612,6 +647,25 @@ static cudaError_t launch_main(const DevBVH& bvh, uint32_t depth, const PbrtRay*
             return any ? launch_persistent<256, true>(bvh, r4, n, order, nullptr, occluded, d_status, stream, replay)
                        : launch_persistent<256, false>(bvh, r4, n, order, h4, nullptr, d_status, stream, replay);
         return cudaErrorInvalidValue;
+    }
+    if (variant == kVariantPairPacket) {
+        if (stack == 64) {
+            if (any)
+                k_trace_packet<64, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status,
+                                                                     replay);
+            else
+                k_trace_packet<64, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status, replay);
+        } else if (stack == 256) {
+            if (any)
+                k_trace_packet<256, true><<<grid, block, 0, stream>>>(bvh, r4, n, order, nullptr, occluded, d_status,
+                                                                      replay);
+            else
+                k_trace_packet<256, false><<<grid, block, 0, stream>>>(bvh, r4, n, order, h4, nullptr, d_status,
+                                                                       replay);
+        } else {
+            return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
     }
     if (stack == 64) {
         if (any)

@@ -494,4 +494,154 @@ __device__ __forceinline__ bool traverse(const DevBVH& bvh, const DRay& r, Trace
 // prim value and rewritten by the replay kernels.
 constexpr int32_t kReplayMark = -2;
 
+// True when every lane of the warp that has a ray (`active`) shares the
+// three direction signs, so that every node orders its children the same
+// way for all of them.  Called by all 32 lanes.
+__device__ __forceinline__ bool warp_signs_uniform(const DRay& r, bool active) {
+    const unsigned s = active ? (r.neg & 7u) : 0u;
+    const unsigned any1 = __reduce_or_sync(0xffffffffu, s);
+    const unsigned all1 = __reduce_and_sync(0xffffffffu, active ? s : 7u);
+    return any1 == all1;
+}
+
+// Warp-cooperative walk of coherent rays, for warps whose rays share their
+// direction signs (warp_signs_uniform); called by all 32 lanes with the SAME
+// tree, `active` false for lanes without a ray.  The warp steps through ONE
+// node at a time, carrying the mask of lanes whose walk visits it: at an
+// inner node every lane of the mask tests both child boxes, the near child
+// (the same for every lane: it depends on the signs only) is taken by the
+// lanes whose near box passed and the far child is pushed with the lanes
+// whose far box passed; at a leaf every lane of the mask tests its
+// primitives.  A popped entry keeps the lanes whose entry distance still
+// passes their own maxt (closest hit) or that have not hit yet (any hit).
+// Each lane so tests exactly the nodes and primitives of its own walk
+// (Traversal::step), in the same order and against the same maxt - the
+// nodes of the walk are a subsequence of the warp's depth-first order, and
+// nothing between two of them changes the lane's state - so its hit, t,
+// barycentrics and NaN flag are the per-lane walk's bit for bit.  Every
+// branch below depends only on the tree and on warp votes, so the warp stays
+// converged at every vote.  Node and primitive records are read at one
+// address by the whole warp.  Trees with instances are not walked here.
+// `*status` gets PBRT_ERR_STACK_OVERFLOW (6) if the stack would overflow
+// (the stack depth is bounded by the tree depth, as per lane).
+template <int STACK, bool ANY>
+__device__ __forceinline__ bool traverse_packet(const DevBVH& bvh, const DRay& r, bool active, TraceResult* res,
+                                                int* status, bool* nan_hit = nullptr) {
+    constexpr unsigned kAll = 0xffffffffu;
+    const unsigned me = 1u << (threadIdx.x & 31u);
+    float maxt = r.tmax;
+    bool found = false, nan = false;
+    res->prim = -1;
+    res->t = 0.0f;
+    res->b1 = 0.0f;
+    res->b2 = 0.0f;
+    if (bvh.empty) return false;
+    float tr;
+    const ChildRec& R = bvh.root;
+    unsigned mask = __ballot_sync(kAll, active && slab(R.lo_x, R.lo_y, R.lo_z, R.hi_x, R.hi_y, R.hi_z, r, maxt, &tr));
+    if (!mask) return false;
+    // the signs of the lowest active lane (equal for every lane by the precondition)
+    const uint32_t neg = __shfl_sync(kAll, r.neg, __ffs(mask) - 1) & 7u;
+    unsigned alive = mask;  // any hit: lanes that have not hit yet
+    uint32_t a = R.a, b = R.b;
+    uint4 st[STACK];  // (child words, entry distance of this lane, lanes that take it)
+    int sp = 0;
+    for (;;) {
+        const bool in = (mask & me) != 0;
+        if (b & kLeafBit) {
+            const uint32_t cnt = b & kCountMask;
+            bool going = in;
+            for (uint32_t i = 0; i < cnt; ++i) {
+                const PrimRec* pr = bvh.prims + a + i;
+                const float4 r0 = ldg4(pr->r0);
+                const uint32_t id = __float_as_uint(r0.w);
+                float t, b1 = 0.0f, b2 = 0.0f;
+                uint32_t add = 0;
+                bool hit = false;
+                if (id & kSphereBit) {
+                    const float4 r1 = ldg4(pr->r1);
+                    if (going)
+                        hit = analytic_test<false, ANY>(bvh.spheres, bvh.insts, __float_as_uint(r1.w), r, maxt, &t, &b1,
+                                                        &b2, &add);
+                } else {
+                    const float4 r1 = ldg4(pr->r1), r2 = ldg4(pr->r2);
+                    if (going) hit = tri_test(r0, r1, r2, r, maxt, &t, &b1, &b2);
+                }
+                if (hit) {
+                    maxt = t;
+                    found = true;
+                    nan |= !(t == t);
+                    res->prim = (int32_t)((id & ~kSphereBit) + add);
+                    res->t = t;
+                    res->b1 = b1;
+                    res->b2 = b2;
+                    if (ANY) going = false;
+                }
+                if (ANY && !__any_sync(kAll, going)) break;
+            }
+            if (ANY) alive &= ~__ballot_sync(kAll, found);
+        } else {
+            const NodePair* np = bvh.pairs + a;
+            const float4 c0a = ldg4(&np->c[0].lo_x), c0b = ldg4(&np->c[0].hi_x);
+            const float4 c1a = ldg4(&np->c[1].lo_x), c1b = ldg4(&np->c[1].hi_x);
+            float t0 = 0.0f, t1 = 0.0f;
+            bool h0 = false, h1 = false;
+            if (in) {
+                if (r.neg & kRayClean) {
+                    h0 = slab_clean(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
+                    h1 = slab_clean(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+                } else {
+                    h0 = slab(c0a.x, c0a.y, c0a.z, c0b.x, c0b.y, c0b.z, r, maxt, &t0);
+                    h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, maxt, &t1);
+                }
+            }
+            // near child: child1 unless dir_is_neg[axis] (bvh.rs:409-415), one choice for the warp
+            const bool swap = (neg >> b) & 1u;
+            const uint32_t na = swap ? __float_as_uint(c1a.w) : __float_as_uint(c0a.w);
+            const uint32_t nb = swap ? __float_as_uint(c1b.w) : __float_as_uint(c0b.w);
+            const uint32_t fa = swap ? __float_as_uint(c0a.w) : __float_as_uint(c1a.w);
+            const uint32_t fb = swap ? __float_as_uint(c0b.w) : __float_as_uint(c1b.w);
+            const unsigned mn = __ballot_sync(kAll, swap ? h1 : h0);
+            const unsigned mf = __ballot_sync(kAll, swap ? h0 : h1);
+            if (mn) {
+                if (mf) {
+                    if (sp == STACK) {
+                        *status = 6;
+                        break;
+                    }
+                    st[sp] = make_uint4(fa, fb, __float_as_uint(swap ? t0 : t1), mf);
+                    ++sp;
+                }
+                a = na;
+                b = nb;
+                mask = mn;
+                continue;
+            }
+            if (mf) {
+                a = fa;
+                b = fb;
+                mask = mf;
+                continue;
+            }
+        }
+        // pop the next deferred child some lane still takes
+        bool got = false;
+        while (sp > 0) {
+            --sp;
+            const uint4 e = st[sp];
+            const unsigned m = e.w & (ANY ? alive : __ballot_sync(kAll, !(__uint_as_float(e.z) > maxt)));
+            if (m) {
+                a = e.x;
+                b = e.y;
+                mask = m;
+                got = true;
+                break;
+            }
+        }
+        if (!got) break;
+    }
+    if (nan_hit) *nan_hit = nan;
+    return found;
+}
+
 }  // namespace pbrt

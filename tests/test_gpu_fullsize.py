@@ -20,7 +20,7 @@ def heightfield():
     return prims, lights, cam, smp, rays
 
 
-@pytest.mark.parametrize("name", ["w4pt", "plain"])
+@pytest.mark.parametrize("name", ["w4pt", "plain", "packet"])
 def test_heightfield_rays_match_oracle(oracle, heightfield, name):
     prims, _, _, _, rays = heightfield
     before = abi.get_trace_config()
@@ -35,10 +35,23 @@ def test_heightfield_rays_match_oracle(oracle, heightfield, name):
         abi.set_trace_config(**before)
 
 
-def test_heightfield_frame_matches_oracle(oracle, heightfield):
+@pytest.fixture(scope="module")
+def heightfield_frame(oracle, heightfield):
     prims, lights, cam, smp, _ = heightfield
     nt = default_num_tasks(cam.film.x_res, cam.film.y_res)
-    gpu = GpuSamplerRenderer(smp, cam, num_tasks=nt).render(GpuScene(prims, lights, 4, "sah"))
-    ref = oracle.render(SceneDescription(prims, lights, 4, "sah"), cam, smp, nt)
+    return oracle.render(SceneDescription(prims, lights, 4, "sah"), cam, smp, nt)
+
+
+@pytest.mark.parametrize("render_kernel", ["plain", "packet", "w4"])
+def test_heightfield_frame_matches_oracle(heightfield, heightfield_frame, render_kernel):
+    prims, lights, cam, smp, _ = heightfield
+    nt = default_num_tasks(cam.film.x_res, cam.film.y_res)
+    before = abi.get_trace_config()
+    abi.set_trace_config(render_kernel=render_kernel)
+    try:
+        gpu = GpuSamplerRenderer(smp, cam, num_tasks=nt).render(GpuScene(prims, lights, 4, "sah"))
+    finally:
+        abi.set_trace_config(**before)
+    ref = heightfield_frame
     assert gpu.shape == (1024, 1024, 3) and ref.max() > 0.1
     assert np.array_equal(gpu.view(np.uint32), ref.view(np.uint32))

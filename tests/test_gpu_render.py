@@ -33,15 +33,26 @@ def assert_image_close(gpu, ref):
     assert ref.max() > 0.1  # the image is not trivially black
 
 
+@pytest.fixture(params=["plain", "packet"])
+def render_kernel(request):
+    """The render's camera and shadow rays through the per-lane walk and
+    through the warp-cooperative one: the same images."""
+    from pbrt_rust_gb300 import abi
+    before = abi.get_trace_config()
+    abi.set_trace_config(render_kernel=request.param)
+    yield request.param
+    abi.set_trace_config(**before)
+
+
 @pytest.mark.parametrize("res", [64, 512])
-def test_c1_render_matches_oracle(oracle, res):
+def test_c1_render_matches_oracle(oracle, res, render_kernel):
     """The plain render (spheres, ground, point + area light, 2x2 strata)."""
     prims, lights, cam, smp = G.c1_scene(res=res)
     gpu, ref = render_both(oracle, prims, lights, cam, smp)
     assert_image_close(gpu, ref)
 
 
-def test_triangle_scene_is_bit_exact(oracle):
+def test_triangle_scene_is_bit_exact(oracle, render_kernel):
     """Without spheres every step is exact IEEE f32: the images are equal."""
     prims, lights, cam, smp = G.c1_scene(res=96, n_spheres=0)
     prims += G.ray_soup(500, 1, seed=5)[0]

@@ -117,7 +117,7 @@ def test_pool_budget_admits_scenes_and_refuses_others(pool):
     resident scenes or their BVHs, and served results stay the ones alone."""
     from pbrt_rust_gb300.batch import batch_bytes
     reqs, alone, scenes = pool
-    lim = dict(max_jobs=64, max_samples=1 << 16, max_film_pixels=1 << 14, max_tasks=1 << 10)
+    lim = dict(max_jobs=64, max_samples=1 << 16, max_film_pixels=1 << 14, max_query_rays=1 << 15, max_tasks=1 << 10)
     slot = batch_bytes(**lim)[0]
     sizes = [sc.device_bytes() for sc in scenes]
     assert all(s > 0 for s in sizes)

@@ -79,7 +79,7 @@ def assert_hits_match(oracle_bvh, got, want, rays, check_f64=True):
             assert abs(got["t"][i] - t64) <= 1e-5 * abs(t64), (i, got["t"][i], t64)
 
 
-KERNELS = ["plain", "pt", "w4", "w4pt", "w4spec"]
+KERNELS = ["plain", "pt", "w4", "w4pt", "w4spec", "packet"]
 
 
 @pytest.fixture(params=KERNELS)
@@ -136,6 +136,36 @@ def test_finite_tmax_and_tmin(soup, oracle, kernel):
     np.testing.assert_array_equal(dev_any(gb, r), ob.intersect_p(r))
 
 
+def octant_sorted(rays):
+    """Rays grouped by their direction signs (stable), so that whole warps
+    share them - the coherent case the packet kernels walk together."""
+    key = (np.signbit(rays["d"]).astype(np.int32) * np.array([1, 2, 4], np.int32)).sum(axis=1)
+    return rays[np.argsort(key, kind="stable")]
+
+
+def test_coherent_rays_match_oracle(soup, oracle, kernel):
+    """Warps of rays with shared direction signs: camera-like bundles from
+    two eye points, sorted by octant, full rays and segments."""
+    prims, _, gb, ob = soup
+    rng = np.random.default_rng(17)
+    n = 1 << 17
+    r = np.zeros(n, dtype=abi.RAY_DTYPE)
+    eye = np.where(rng.uniform(size=(n, 1)) < 0.5, [0.1, 0.2, -3.0], [2.5, -0.3, 0.4]).astype(np.float32)
+    tgt = rng.uniform(-0.6, 0.6, size=(n, 3)).astype(np.float32)
+    d = tgt - eye
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r["o"] = eye
+    r["d"] = d
+    r["tmin"] = 1e-4
+    r["tmax"] = np.float32(np.inf)
+    r["tmax"][::7] = np.float32(2.5)  # some segments
+    r = octant_sorted(r)
+    want = ob.intersect(r)
+    assert (want["prim"] >= 0).mean() > 0.2
+    assert_hits_match(ob, dev_hits(gb, r), want, r)
+    np.testing.assert_array_equal(dev_any(gb, r), ob.intersect_p(r))
+
+
 @pytest.mark.parametrize("sm", ["middle", "equal"])
 def test_other_split_methods(oracle, sm, kernel):
     prims, rays = G.ray_soup(2000, 1 << 16, seed=11)
@@ -153,6 +183,7 @@ def test_sphere_scene_matches_oracle(oracle, kernel):
     ob = oracle.OracleBVH(prims, 4, "sah")
     rng = G.PCG32(99)
     rays = G.incoherent_rays(rng, 1 << 18, (-4, 0, -4), (4, 3, 4))
+    rays[: 1 << 17] = octant_sorted(rays[: 1 << 17])  # half of them in sign-coherent warps
     want = ob.intersect(rays)
     got = dev_hits(gb, rays)
     assert (want["prim"] >= 1).sum() > 1000
