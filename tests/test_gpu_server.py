@@ -121,21 +121,23 @@ def test_pool_budget_admits_scenes_and_refuses_others(pool):
     slot = batch_bytes(**lim)[0]
     sizes = [sc.device_bytes() for sc in scenes]
     assert all(s > 0 for s in sizes)
-    budget = 2 * slot + sum(sizes[:4])  # room for four of the five scenes
+    out = min(range(len(scenes)), key=lambda k: sizes[k])  # the scene left out: the smallest
+    kept = [k for k in range(len(scenes)) if k != out]
+    budget = 2 * slot + sum(sizes[k] for k in kept)  # full once the others are resident
     srv = GpuServer(slots=2, pool_bytes=budget, **lim)
     try:
-        for sc in scenes[:4]:
-            srv.admit(sc)
+        for k in kept:
+            srv.admit(scenes[k])
         with pytest.raises(abi.PbrtError) as e:
-            srv.admit(scenes[4])
+            srv.admit(scenes[out])
         assert e.value.status == abi.PBRT_ERR_BUDGET
         st = srv.stats()
         assert st["pool_bytes"] == budget and st["slot_bytes"] == 2 * slot
-        assert st["resident_bytes"] == sum(sizes[:4]) and st["resident_count"] == 4
+        assert st["resident_bytes"] == sum(sizes[k] for k in kept) and st["resident_count"] == len(kept)
         tickets = []
         for r, want in zip(reqs, alone):
             sc_index = next(k for k, sc in enumerate(scenes) if (r[1] is sc or getattr(r[1], "_owner", None) is sc))
-            if sc_index == 4:
+            if sc_index == out:
                 with pytest.raises(abi.PbrtError) as e:
                     submit(srv, r)
                 assert e.value.status == abi.PBRT_ERR_BUDGET
@@ -143,9 +145,9 @@ def test_pool_budget_admits_scenes_and_refuses_others(pool):
                 tickets.append((submit(srv, r), want))
         for t, want in tickets:
             assert np.array_equal(bits(srv.wait(t)), bits(want))
-        assert srv.stats()["refused"] == 3  # the fifth scene's two renders and query
-        srv.release(scenes[0])
-        srv.admit(scenes[4])  # now it fits
-        assert srv.stats()["resident_bytes"] == sum(sizes[1:5])
+        assert srv.stats()["refused"] == 3  # the left-out scene's two renders and query
+        srv.release(scenes[kept[0]])
+        srv.admit(scenes[out])  # it fits in the room of any larger scene
+        assert srv.stats()["resident_bytes"] == sum(sizes[k] for k in kept[1:]) + sizes[out]
     finally:
         srv.close()
