@@ -207,46 +207,26 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
         base = __shfl_sync(kFull, base, 0);
         if ((uint64_t)base >= n) break;
         const uint64_t end = (uint64_t)base + chunk < n ? (uint64_t)base + chunk : n;
-        for (uint64_t wbase = (uint64_t)base; wbase < end; wbase += 32u) {  // warp-uniform
-            const uint64_t my = wbase + lane;
-            const bool active = my < end;
-            uint32_t job = 0;
-            uint64_t item = 0;  // extend: index inside the job; shadow: queue entry
-            const float4* src = nullptr;
-            if (active) {
-                if (SHADOW) {
-                    job = __ldg(A.q_job + my);
-                    item = my;
-                    src = reinterpret_cast<const float4*>(A.q_rays) + 2 * my;
-                } else {
-                    job = locate(A.off_ray, nj, my, c);
-                    item = my - c.lo;
-                    src = A.jobs[job].rays + 2 * item;
-                }
+        for (uint64_t my = (uint64_t)base + lane; my < end; my += 32u) {
+            uint32_t job;
+            uint64_t item;  // extend: index inside the job; shadow: queue entry
+            const float4* src;
+            if (SHADOW) {
+                job = __ldg(A.q_job + my);
+                item = my;
+                src = reinterpret_cast<const float4*>(A.q_rays) + 2 * my;
+            } else {
+                job = locate(A.off_ray, nj, my, c);
+                item = my - c.lo;
+                src = A.jobs[job].rays + 2 * item;
             }
-            // lane 0 always has a ray (wbase < end); lanes without one stand
-            // in with lane 0's job, so that a warp walking together reads one
-            // tree in every lane
-            const uint32_t job0 = __shfl_sync(kFull, job, 0);
-            if (!active) job = job0;
             const JobRec& J = A.jobs[job];
             const bool any = MODE == kAny || (MODE == kPerJob && J.any != 0);
-            const DRay r = active ? make_dray(__ldg(src), __ldg(src + 1))
-                                  : make_dray(make_float4(0, 0, 0, 0), make_float4(0, 0, 1, 0));
+            const DRay r = make_dray(__ldg(src), __ldg(src + 1));
             TraceResult res;
             int fail = 0;
-            bool nan = false, found = false;
-            // a warp of one render job's rays (camera or shadow rays: coherent)
-            // sharing their direction signs walks them together over the
-            // binary layout; the answers are the per-lane walks'
-            const bool packet = __all_sync(kFull, job == job0 && J.kind == kJobRender && J.P.depth <= 64 &&
-                                                      J.P.bvh.insts == nullptr && (SHADOW || !any)) &&
-                                warp_signs_uniform(r, active);
-            if (packet) {
-                found = SHADOW ? traverse_packet<64, true>(J.P.bvh, r, active, &res, &fail)
-                               : traverse_packet<64, false>(J.P.bvh, r, active, &res, &fail, &nan);
-            } else if (!active) {
-            } else if (WIDE) {
+            bool nan = false, found;
+            if (WIDE) {
                 Traversal4<S1, S2> T;
                 T.bind(smem_stack, threadIdx.x, blockDim.x);
                 const DevBVH4 bv = J.P.bvh4;
@@ -268,7 +248,6 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
                 found = any ? traverse<S1, true, S2 != 0>(bv, r, &res, &fail)
                             : traverse<S1, false, S2 != 0>(bv, r, &res, &fail, &nan);
             }
-            if (!active) continue;
             if (fail) atomicMax((int*)(J.P.counters + 2), fail);
             if (SHADOW) {
                 J.P.occluded[__ldg(A.q_slot + item)] = found ? 1 : 0;

@@ -20,6 +20,7 @@ float32.
 from __future__ import annotations
 
 import dataclasses
+import functools
 import math
 
 import numpy as np
@@ -51,6 +52,7 @@ class PCG32:
         self.state = (self.state * _MUL + self.inc) & _MASK
 
     @staticmethod
+    @functools.lru_cache(maxsize=16)
     def _jump_tables(n: int, inc: int):
         """A^k and C_k (k = 0..n-1) with s_k = A^k s_0 + C_k (mod 2^64)."""
         a = np.empty(n, dtype=np.uint64)

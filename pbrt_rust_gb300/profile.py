@@ -48,16 +48,14 @@ def serving_pool(n_scenes: int = 32, threads: int = 8):
 
 def serving_requests(pool, n_requests: int, device, seed: int | None = None):
     """The request stream over `pool`: ("render", scene, renderer, out) or
-    ("query", bvh, rays, out) tuples, rays and outputs on `device`.  Ray
-    batches of the same scene and size share one ray array (each request
-    has its own output)."""
+    ("query", bvh, rays, out) tuples, rays and outputs on `device`; every
+    ray batch has its own rays."""
     import torch
 
     from . import generators as G
     from .gpu import GpuSamplerRenderer
     from .scene import Camera, Film, Filter, StratifiedSampler
     reqs = []
-    ray_sets = {}
     for spec in G.serving_requests(n_requests, len(pool), seed=seed):
         sc, bvh, cam = pool[spec["scene"]]
         if spec["kind"] == "render":
@@ -68,12 +66,10 @@ def serving_requests(pool, n_requests: int, device, seed: int | None = None):
             smp = StratifiedSampler.stratified(0, res, 0, res, side, side, True, 0.0, 1.0)
             reqs.append(("render", sc, GpuSamplerRenderer(smp, c), torch.empty((res, res, 3), device=device)))
         else:
-            key = (spec["scene"], spec["n"])
-            if key not in ray_sets:
-                lo, hi = bvh.world_bound()
-                rays = G.incoherent_rays(G.PCG32(spec["seed"]), spec["n"], lo, hi)
-                ray_sets[key] = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(device)
-            reqs.append(("query", bvh, ray_sets[key], torch.empty((spec["n"], 4), device=device)))
+            lo, hi = bvh.world_bound()
+            rays = G.incoherent_rays(G.PCG32(spec["seed"]), spec["n"], lo, hi)
+            rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(device)
+            reqs.append(("query", bvh, rd, torch.empty((spec["n"], 4), device=device)))
     return reqs
 
 
