@@ -47,112 +47,53 @@ __device__ __forceinline__ uint32_t locate(const uint64_t* __restrict__ off, uin
     return lo;
 }
 
-constexpr unsigned kAll = 0xffffffffu;
-
-// The job parameters of a warp's items in the warp's shared-memory slot.
-// In global memory every field read after one of the stage's stores had to
-// be read again (the compiler cannot rule out that the store changed it);
-// shared memory cannot alias those stores, so each field is read once, much
-// as the single-render kernels read theirs from the constant bank.  Calls
-// f(P, mine) with every lane of the warp once per distinct job among the
-// lanes that have an item (almost always one round): `mine` marks the lanes
-// whose item belongs to that round's job.  The slot keeps its job between
-// calls (*held, warp-uniform; ~0u: none).
-template <class F>
-__device__ __forceinline__ void per_job(const BatchArgs& A, RenderParams* slot, uint32_t* held, bool live, uint32_t j,
-                                        F&& f) {
-    const unsigned lane = threadIdx.x & 31u;
-    unsigned todo = __ballot_sync(kAll, live);
-    while (todo) {
-        const uint32_t jj = __shfl_sync(kAll, j, __ffs(todo) - 1);
-        if (jj != *held) {
-            __syncwarp();
-            const uint32_t* src = reinterpret_cast<const uint32_t*>(&A.jobs[jj].P);
-            uint32_t* dst = reinterpret_cast<uint32_t*>(slot);
-            for (uint32_t k = lane; k < sizeof(RenderParams) / 4; k += 32) dst[k] = __ldg(src + k);
-            __syncwarp();
-            *held = jj;
-        }
-        const bool mine = live && j == jj;
-        f(*slot, mine);
-        todo &= ~__ballot_sync(kAll, mine);
-    }
-}
-
-static_assert(sizeof(RenderParams) % 4 == 0, "RenderParams is copied as words");
-
-// Every stage loop below is block-uniform: each warp runs per_job's rounds
-// (and shade_sample's warp-aggregated append) with all of its lanes.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_generate(BatchArgs A) {
     __shared__ uint32_t words[32 * BLOCK];  // the threads' ChaCha block pairs
-    __shared__ RenderParams slots[BLOCK / 32];
     const uint64_t total = A.hdr->pix;
     const uint32_t nj = A.hdr->n_jobs;
-    uint32_t held = ~0u;
     Cursor c{0, 1, 0};
-    for (uint64_t base = (uint64_t)blockIdx.x * BLOCK; base < total; base += (uint64_t)gridDim.x * BLOCK) {
-        const uint64_t g = base + threadIdx.x;
-        const bool live = g < total;
-        const uint32_t j = live ? locate(A.off_pix, nj, g, c) : 0u;
-        const uint32_t item = live ? (uint32_t)(g - c.lo) : 0u;
-        per_job(A, slots + threadIdx.x / 32, &held, live, j, [&](const RenderParams& P, bool mine) {
-            if (mine) generate_pixel(P, item, words + threadIdx.x, (uint32_t)BLOCK);
-        });
+    for (uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; g < total; g += (uint64_t)gridDim.x * BLOCK) {
+        const uint32_t j = locate(A.off_pix, nj, g, c);
+        generate_pixel(A.jobs[j].P, (uint32_t)(g - c.lo), words + threadIdx.x, (uint32_t)BLOCK);
     }
 }
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_shade(BatchArgs A) {
-    __shared__ RenderParams slots[BLOCK / 32];
     const uint64_t total = A.hdr->samples;
     const uint32_t nj = A.hdr->n_jobs;
     const ShadowSink Q{A.q_rays, A.q_slot, A.q_job, A.counters + kCtrShadowCount};
-    uint32_t held = ~0u;
     Cursor c{0, 1, 0};
+    // the block-uniform loop keeps whole warps together for shade_sample's
+    // warp-aggregated queue append
     for (uint64_t base = (uint64_t)blockIdx.x * BLOCK; base < total; base += (uint64_t)gridDim.x * BLOCK) {
         const uint64_t g = base + threadIdx.x;
         const bool live = g < total;
         const uint32_t j = live ? locate(A.off_smp, nj, g, c) : 0u;
-        const uint64_t item = live ? g - c.lo : 0u;
-        per_job(A, slots + threadIdx.x / 32, &held, live, j,
-                [&](const RenderParams& P, bool mine) { shade_sample(P, mine ? item : 0u, mine, Q, j); });
+        shade_sample(A.jobs[j].P, live ? g - c.lo : 0u, live, Q, j);
     }
 }
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_combine(BatchArgs A) {
-    __shared__ RenderParams slots[BLOCK / 32];
     const uint64_t total = A.hdr->samples;
     const uint32_t nj = A.hdr->n_jobs;
-    uint32_t held = ~0u;
     Cursor c{0, 1, 0};
-    for (uint64_t base = (uint64_t)blockIdx.x * BLOCK; base < total; base += (uint64_t)gridDim.x * BLOCK) {
-        const uint64_t g = base + threadIdx.x;
-        const bool live = g < total;
-        const uint32_t j = live ? locate(A.off_smp, nj, g, c) : 0u;
-        const uint64_t item = live ? g - c.lo : 0u;
-        per_job(A, slots + threadIdx.x / 32, &held, live, j, [&](const RenderParams& P, bool mine) {
-            if (mine) combine_sample(P, item);
-        });
+    for (uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; g < total; g += (uint64_t)gridDim.x * BLOCK) {
+        const uint32_t j = locate(A.off_smp, nj, g, c);
+        combine_sample(A.jobs[j].P, g - c.lo);
     }
 }
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_film(BatchArgs A) {
-    __shared__ RenderParams slots[BLOCK / 32];
     const uint64_t total = A.hdr->film;
     const uint32_t nj = A.hdr->n_jobs;
-    uint32_t held = ~0u;
     Cursor c{0, 1, 0};
-    for (uint64_t base = (uint64_t)blockIdx.x * BLOCK; base < total; base += (uint64_t)gridDim.x * BLOCK) {
-        const uint64_t g = base + threadIdx.x;
-        const bool live = g < total;
-        const uint32_t j = live ? locate(A.off_film, nj, g, c) : 0u;
-        const uint32_t item = live ? (uint32_t)(g - c.lo) : 0u;
-        per_job(A, slots + threadIdx.x / 32, &held, live, j, [&](const RenderParams& P, bool mine) {
-            if (mine) film_pixel(P, item);
-        });
+    for (uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; g < total; g += (uint64_t)gridDim.x * BLOCK) {
+        const uint32_t j = locate(A.off_film, nj, g, c);
+        film_pixel(A.jobs[j].P, (uint32_t)(g - c.lo));
     }
 }
 
