@@ -187,9 +187,7 @@ __global__ void __launch_bounds__(BLOCK) kb_trace(BatchArgs A) {
 // kb_trace with refill = 32, where a warp takes new rays only once all of
 // its lanes are done: each lane walks its ray to the end in the
 // single-scene kernels' loop, with no warp vote per traversal step and only
-// the fields of the job's tree the walk reads held in registers.  In a
-// 4-wide stage the rays of render jobs whose tree a 64-entry stack covers
-// walk the binary layout, as the single-render kernels do.  The same
+// the fields of the job's tree the walk reads held in registers.  The same
 // rays go to the same warps in the same groups, each walked in the same
 // order, so the results equal kb_trace's (measured on GB300, the
 // 1024x1024x16 heightfield frame as one job: extend 3.47 -> 2.3 ms, shadow
@@ -228,14 +226,7 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
             TraceResult res;
             int fail = 0;
             bool nan = false, found;
-            // render jobs' camera and shadow rays are coherent and walk the
-            // binary layout faster (as the single-render kernels do); query
-            // rays take the stage's layout
-            const bool pair64 = WIDE && J.kind == kJobRender && J.P.depth <= 64;
-            if (pair64) {
-                found = any ? traverse<64, true>(J.P.bvh, r, &res, &fail)
-                            : traverse<64, false>(J.P.bvh, r, &res, &fail, &nan);
-            } else if (WIDE) {
+            if (WIDE) {
                 Traversal4<S1, S2> T;
                 T.bind(smem_stack, threadIdx.x, blockDim.x);
                 const DevBVH4 bv = J.P.bvh4;
