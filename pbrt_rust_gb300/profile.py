@@ -112,6 +112,7 @@ def main(argv=None) -> int:
     ap.add_argument("--spp-side", type=int, default=2)
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--slots", type=int, default=2)
+    ap.add_argument("--tuning", default="", help="served: batch tuning as key=value,... (GpuServer tuning)")
     a = ap.parse_args(argv)
     import torch
 
@@ -133,8 +134,10 @@ def main(argv=None) -> int:
         t0 = time.perf_counter()
         run_plain(reqs, stream)
         plain_s = time.perf_counter() - t0
-        srv = GpuServer(slots=a.slots, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22,
-                        max_query_rays=1 << 20, max_tasks=1 << 14)
+        tuning = {k: (v if k.endswith("kernel") else int(v))
+                  for k, v in (kv.split("=") for kv in a.tuning.split(",") if kv)}
+        srv = GpuServer(slots=a.slots, tuning=tuning or None, max_jobs=256, max_samples=1 << 24,
+                        max_film_pixels=1 << 22, max_query_rays=1 << 20, max_tasks=1 << 14)
         outs = [torch.empty_like(r[3]) for r in reqs]
         for _ in range(a.repeat):
             st = run_served(srv, reqs, outs)
