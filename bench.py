@@ -251,13 +251,22 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000,
     from pbrt_rust_gb300.profile import run_plain, run_served, serving_pool, serving_requests
     from pbrt_rust_gb300.server import GpuServer
 
+    from pbrt_rust_gb300 import abi
     pool = serving_pool(n_scenes)
     reqs = serving_requests(pool, n_requests, dev)
-    run_plain(reqs[:20], stream)
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    run_plain(reqs, stream)
-    plain_s = time.perf_counter() - t0
+    # the plain path with each render kernel (identical outputs): the
+    # library's default and the 4-wide walk, which these scenes favour
+    before = abi.get_trace_config()
+    plain_s = {}
+    for rk in ("plain", "w4"):
+        abi.set_trace_config(render_kernel=rk)
+        run_plain(reqs[:20], stream)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        run_plain(reqs, stream)
+        plain_s[rk] = time.perf_counter() - t0
+    abi.set_trace_config(**before)
+    default_rk = before["render_kernel"] if before["render_kernel"] in plain_s else "plain"
     ref = [r[3].clone() for r in reqs]
     srv = GpuServer(slots=slots, pool_bytes=POOL_BYTES, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22,
                     max_query_rays=1 << 20, max_tasks=1 << 14)
@@ -281,9 +290,11 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000,
     srv.close()
     n_render = sum(1 for r in reqs if r[0] == "render")
     return {"scenes": n_scenes, "requests": len(reqs), "renders": n_render, "queries": len(reqs) - n_render,
-            "slots": slots, "plain_requests_per_s": len(reqs) / plain_s,
+            "slots": slots, "plain_requests_per_s": len(reqs) / plain_s[default_rk],
+            "plain_requests_per_s_by_render_kernel": {k: len(reqs) / v for k, v in plain_s.items()},
             "served_requests_per_s": flood["requests_per_s"],
-            "speedup": flood["requests_per_s"] * plain_s / len(reqs),
+            "speedup": flood["requests_per_s"] * plain_s[default_rk] / len(reqs),
+            "speedup_vs_fastest_plain": flood["requests_per_s"] * min(plain_s.values()) / len(reqs),
             "flood_p50_ms": flood["p50_ms"], "flood_p99_ms": flood["p99_ms"],
             "flood_mean_batch": flood["mean_batch_requests"], "flood_deferred": flood["deferred"],
             "pool": {"budget_bytes": POOL_BYTES, "slot_bytes": final["slot_bytes"],
