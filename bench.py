@@ -9,12 +9,12 @@ on the sphere).  One step = one closest-hit pass over all 2^22 rays.
   value       device-resident rays/hits, kernel time from CUDA events on
               the launching stream; L2 flushed (256 MiB write) between steps
   e2e         the same pass through the C ABI with pinned HOST buffers and
-              the synchronisation inside the timed step: the traversal reads
-              the rays from and writes the hits to the mapped host memory
-              (Grace memory over NVLink-C2C); `e2e.staged` is the same call
-              with PBRT_HOST_MAPPED=0, i.e. host->device copies of the rays,
-              traversal and device->host copies of the hits pipelined in
-              four pieces
+              the synchronisation inside the timed step, in the library's
+              default form (host->device copies of the rays, traversal and
+              device->host copies of the hits pipelined in four pieces);
+              `e2e.forms` also times PBRT_HOST_MAPPED=1, where the traversal
+              reads the rays from and writes the hits to the mapped host
+              memory (Grace memory over NVLink-C2C), alternating rounds
   roofline    algorithmic bytes per launch (32 B per node tested + 48 B per
               triangle tested + 32 B ray + 16 B hit, counted by the oracle's
               reference-order traversal on a 2^16-ray sample and scaled)
@@ -685,8 +685,8 @@ def run_ours(args):
 
     print(f"[bench] closest {statistics.mean(ms_closest):.3f} ms/step, any {statistics.mean(ms_any):.3f} ms/step",
           file=sys.stderr, flush=True)
-    # e2e: pinned host buffers through the C ABI, read and written in place
-    # (default) or staged through device copies (PBRT_HOST_MAPPED=0)
+    # e2e: pinned host buffers through the C ABI, staged through device
+    # copies (default, PBRT_HOST_MAPPED=0) or read and written in place (=1)
     rays_host = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
     hits_host = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
     rh, hh = C.c_void_p(rays_host.data_ptr()), C.c_void_p(hits_host.data_ptr())

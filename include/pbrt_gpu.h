@@ -260,9 +260,10 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* bvh, uint32_t* out,
 
 /* Replaces Intersectable::intersect for the BVH (bvh.rs:375-422) over a
  * batch of rays: closest hit per ray.  rays/hits may be device pointers
- * or host pointers (pinned or pageable).  Pinned host buffers are mapped
- * into the device's address space and the traversal on `stream` reads and
- * writes them in place (PBRT_HOST_MAPPED=0 stages them like pageable ones).
+ * or host pointers (pinned or pageable).  Host buffers are staged through
+ * the device as below; with PBRT_HOST_MAPPED=1 pinned host buffers are
+ * instead mapped into the device's address space and the traversal on
+ * `stream` reads and writes them in place.
  * Pageable buffers are staged through the device: the traversal on
  * `stream` (after the work queued on it) and, for 2^19 rays or more, the
  * copies (and every other piece's traversal) on the handle's own streams

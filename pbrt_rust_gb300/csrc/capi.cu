@@ -228,15 +228,16 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
 }
 
 // Pinned host memory is mapped into the device's address space (on GB300
-// it is the Grace memory behind NVLink-C2C): the traversal then reads the
-// rays and writes the results there directly, with no staging copies.
-// Measured with 2^22 heightfield rays in pinned buffers: closest hit 1.63 ms
-// against 1.75 ms through the copy pipeline below, any hit 1.24 against
-// 1.43 ms, identical results.  PBRT_HOST_MAPPED=0 (read at every call)
-// takes the copy pipeline.
+// it is the Grace memory behind NVLink-C2C).  With PBRT_HOST_MAPPED=1 (read
+// at every call) the traversal reads the rays and writes the results there
+// directly, with no staging copies; by default pinned buffers take the copy
+// pipeline below.  Measured with 2^22 heightfield rays in pinned buffers on
+// several GB300 machines: in place 1.60-1.82 ms per call depending on the box
+// (2306-2614 Mrays/s), the copy pipeline 1.74-1.75 ms on every box (2403-2414
+// Mrays/s); the pipeline has the better worst case.  Identical results.
 static bool host_mapped_enabled() {
     const char* v = getenv("PBRT_HOST_MAPPED");
-    return !(v && v[0] == '0');
+    return v && v[0] == '1';
 }
 // The device address of a pinned, mapped host allocation, else nullptr.
 static void* mapped_host_pointer(const void* p) {

@@ -422,10 +422,10 @@ def test_pipelined_host_buffers_equal_device_buffers():
 
 @pytest.mark.gpu
 def test_pinned_host_buffers_in_place_and_staged(monkeypatch):
-    """Pinned host buffers are read and written in place by the traversal
-    (mapped host memory); PBRT_HOST_MAPPED=0 stages them through device
-    copies instead.  Both, and a pinned/device mix, give the device-buffer
-    results bit for bit."""
+    """Pinned host buffers are staged through device copies by default and
+    read and written in place by the traversal (mapped host memory) with
+    PBRT_HOST_MAPPED=1.  Both, and a pinned/device mix, give the
+    device-buffer results bit for bit."""
     torch = _torch()
     prims, _ = G.ray_soup(4096, 1, seed=5)
     g = GpuBVHAccel(prims, 4, "sah")
