@@ -428,7 +428,13 @@ struct Traversal {
                 h1 = slab(c1a.x, c1a.y, c1a.z, c1b.x, c1b.y, c1b.z, r, lim, &t1);
             }
             // Near child: child1 unless dir_is_neg[axis] (bvh.rs:409-415).
-            bool swap = (r.neg >> b) & 1u;
+            // An any-hit walk may take its children in any order - its
+            // answer is whether some primitive whose boxes all pass against
+            // the ray's own maxt is hit, whatever the order - so it takes the
+            // child whose box it enters first, which meets an occluder near
+            // the ray's origin sooner (on shadow rays of the serving scenes
+            // the oracle counts ~11 % fewer nodes to the first hit).
+            bool swap = (ANY && !EXACT) ? (h1 && (!h0 || t1 < t0)) : ((r.neg >> b) & 1u);
             uint32_t na = swap ? __float_as_uint(c1a.w) : __float_as_uint(c0a.w);
             uint32_t nb = swap ? __float_as_uint(c1b.w) : __float_as_uint(c0b.w);
             uint32_t fa = swap ? __float_as_uint(c0a.w) : __float_as_uint(c1a.w);
