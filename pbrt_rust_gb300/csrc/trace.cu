@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(128)
                 kept = T.cur;
                 live = T.pop();
             } else {
-                live = T.node(bvh, r);
+                live = T.template node<ANY>(bvh, r);
                 if (T.overflow) finish();
             }
         }

@@ -314,12 +314,13 @@ struct Traversal4 : InstWalk<INST> {
             if (INST && st == 2) return !overflow;
             return pop();
         }
-        return node(bvh, r);
+        return node<ANY>(bvh, r);
     }
 
     // Visits inner node `cur`: tests its children and moves `cur` to the
-    // next node or leaf in the reference's order; false once nothing is
-    // left.
+    // next node or leaf in the reference's order (an any-hit walk: nearest
+    // entry first); false once nothing is left.
+    template <bool ANY>
     __device__ __forceinline__ bool node(const DevBVH4& bvh, const DRay& r) {
         const Node4* nd = node_base(bvh) + cur;
         ChildV c0, c1, c2, c3;
@@ -356,10 +357,28 @@ struct Traversal4 : InstWalk<INST> {
         // into visit order (bvh.rs:409-415): each child's pair of children
         // by that child's axis sign, then the two pairs by N's
         uint32_t a0 = c0.a, a1 = c1.a, a2 = c2.a, a3 = c3.a;
-        cswap(sL, a0, a1, h0, h1, t0, t1);
-        cswap(sR, a2, a3, h2, h3, t2, t3);
-        cswap(sN, a0, a2, h0, h2, t0, t2);
-        cswap(sN, a1, a3, h1, h3, t1, t3);
+        if (ANY && !EXACT) {
+            // An any-hit walk's answer does not depend on the order it takes
+            // children in (some primitive whose boxes all pass the ray's own
+            // maxt is hit, or none is), so it takes them by entry distance:
+            // an occluder near the ray's origin is met sooner.  Children that
+            // fail sort last; a five-comparator network sorts the four.
+            const float inf = __int_as_float(0x7f800000);
+            t0 = h0 ? t0 : inf;
+            t1 = h1 ? t1 : inf;
+            t2 = h2 ? t2 : inf;
+            t3 = h3 ? t3 : inf;
+            cswap(t0 > t1, a0, a1, h0, h1, t0, t1);
+            cswap(t2 > t3, a2, a3, h2, h3, t2, t3);
+            cswap(t0 > t2, a0, a2, h0, h2, t0, t2);
+            cswap(t1 > t3, a1, a3, h1, h3, t1, t3);
+            cswap(t1 > t2, a1, a2, h1, h2, t1, t2);
+        } else {
+            cswap(sL, a0, a1, h0, h1, t0, t1);
+            cswap(sR, a2, a3, h2, h3, t2, t3);
+            cswap(sN, a0, a2, h0, h2, t0, t2);
+            cswap(sN, a1, a3, h1, h3, t1, t3);
+        }
         if (EXACT) {
             // replay: the reference takes the first child whose box passes
             // maxt now, culls the ones before it now, and tests the pushed
