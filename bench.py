@@ -10,11 +10,14 @@ on the sphere).  One step = one closest-hit pass over all 2^22 rays.
               the launching stream; L2 flushed (256 MiB write) between steps
   e2e         the same pass through the C ABI with pinned HOST buffers and
               the synchronisation inside the timed step, in the library's
-              default form (host->device copies of the rays, traversal and
-              device->host copies of the hits pipelined in four pieces);
-              `e2e.forms` also times PBRT_HOST_MAPPED=1, where the traversal
-              reads the rays from and writes the hits to the mapped host
-              memory (Grace memory over NVLink-C2C), alternating rounds
+              default form (streamed: one traversal launch whose warps wait
+              for the ray pieces copied in behind it, the hits written to
+              the host by the walk chunk by chunk); `e2e.forms` also times
+              the copy pipeline (PBRT_STREAM_IN=0: copies in, traversal and
+              copies out in four overlapped pieces) and PBRT_HOST_MAPPED=1,
+              where the traversal reads the rays from and writes the hits to
+              the mapped host memory (Grace memory over NVLink-C2C), in
+              alternating rounds; `e2e.any_hit_forms` the same for any hit
   roofline    algorithmic bytes per launch (32 B per node tested + 48 B per
               triangle tested + 32 B ray + 16 B hit, counted by the oracle's
               reference-order traversal on a 2^16-ray sample and scaled)
@@ -693,32 +696,45 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     hits_want = hits_dev.cpu().view(torch.int32)
 
-    def e2e_pass(mapped) -> float:  # None: the library's default form
-        if mapped is None:
-            os.environ.pop("PBRT_HOST_MAPPED", None)
-        else:
-            os.environ["PBRT_HOST_MAPPED"] = "1" if mapped else "0"
+    occ_host = torch.empty((N_RAYS,), dtype=torch.uint8).pin_memory()
+    oh = C.c_void_p(occ_host.data_ptr())
+    occ_want = occ_dev.cpu()
+    form_env = {"default": {}, "pipelined": {"PBRT_STREAM_IN": "0"}, "in_place": {"PBRT_HOST_MAPPED": "1"}}
+
+    def e2e_pass(form, any_hit=False) -> float:
+        for k in ("PBRT_STREAM_IN", "PBRT_HOST_MAPPED"):
+            os.environ.pop(k, None)
+        os.environ.update(form_env[form])
+
+        def call():
+            if any_hit:
+                abi.check(lib.pbrtgpu_intersect_p(bvh._h, rh, N_RAYS, oh, sh), lib)
+            else:
+                abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
         for _ in range(args.warmup):
-            abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
+            call()
         t = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            abi.check(lib.pbrtgpu_intersect(bvh._h, rh, N_RAYS, hh, sh), lib)
+            call()
             t.append(time.perf_counter() - t0)
         # the host copy of the result must equal the device-resident one
-        if not torch.equal(hits_host.view(torch.int32), hits_want):
-            raise RuntimeError("host-buffer and device-buffer hits differ")
+        if not (torch.equal(occ_host, occ_want) if any_hit else torch.equal(hits_host.view(torch.int32), hits_want)):
+            raise RuntimeError(f"host-buffer and device-buffer results differ ({form})")
         hits_host.zero_()
+        occ_host.fill_(7)
         return N_RAYS / statistics.mean(t) / 1e6
 
-    # the default and the two host-buffer forms alternate over a few rounds
-    runs = {"default": [], "staged": [], "in_place": []}
+    # the default and the other host-buffer forms alternate over a few rounds
+    runs = {k: [] for k in form_env}
+    any_runs = {k: [] for k in form_env}
     for _ in range(4):
-        runs["default"].append(e2e_pass(None))
-        runs["staged"].append(e2e_pass(False))
-        runs["in_place"].append(e2e_pass(True))
+        for k in form_env:
+            runs[k].append(e2e_pass(k))
+            any_runs[k].append(e2e_pass(k, any_hit=True))
     e2e_mrays = statistics.median(runs["default"])
-    os.environ.pop("PBRT_HOST_MAPPED", None)
+    for k in ("PBRT_STREAM_IN", "PBRT_HOST_MAPPED"):
+        os.environ.pop(k, None)
 
     # render of the same scene: 1024x1024, 16 spp, direct lighting
     c2, _ = bench_render(torch, dev, stream, flush, prims, lights, cam, smp, frames=5)
@@ -769,10 +785,16 @@ def run_ours(args):
                     "how": "median of 4 rounds of the library's default form, pinned host buffers",
                     "forms": {k: {"median": statistics.median(v), "min": min(v), "max": max(v), "runs": v}
                               for k, v in runs.items()},
-                    "form_meaning": {"in_place": "PBRT_HOST_MAPPED=1: the traversal reads the rays from and "
+                    "any_hit_forms": {k: {"median": statistics.median(v), "min": min(v), "max": max(v)}
+                                      for k, v in any_runs.items()},
+                    "form_meaning": {"default": "streamed: one traversal launch; the rays follow in pieces on a "
+                                                "copy stream and warps wait for the piece they take; closest hits "
+                                                "are staged on the device and written to the host by the walk, "
+                                                "chunk by chunk in coalesced rows",
+                                     "in_place": "PBRT_HOST_MAPPED=1: the traversal reads the rays from and "
                                                  "writes the hits to the mapped host memory",
-                                     "staged": "PBRT_HOST_MAPPED=0: H2D copy, traversal, D2H copy in 4 "
-                                               "overlapped pieces"}},
+                                     "pipelined": "PBRT_STREAM_IN=0: H2D copy, traversal, D2H copy in 4 "
+                                                  "overlapped pieces"}},
             # per timed step: the traversal kernel and the replay check (D24)
             "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),

@@ -260,17 +260,24 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* bvh, uint32_t* out,
 
 /* Replaces Intersectable::intersect for the BVH (bvh.rs:375-422) over a
  * batch of rays: closest hit per ray.  rays/hits may be device pointers
- * or host pointers (pinned or pageable).  Host buffers are staged through
- * the device as below; with PBRT_HOST_MAPPED=1 pinned host buffers are
- * instead mapped into the device's address space and the traversal on
- * `stream` reads and writes them in place.
- * Pageable buffers are staged through the device: the traversal on
- * `stream` (after the work queued on it) and, for 2^19 rays or more, the
- * copies (and every other piece's traversal) on the handle's own streams
- * in PBRT_PIPE_CHUNKS (default 4) pieces that overlap the traversal of the
- * others.  The call returns after the work is queued for device buffers
- * and after completion for host buffers.  `stream` is a cudaStream_t
- * (NULL = legacy default stream). */
+ * or host pointers (pinned or pageable).  Host buffers take one of three
+ * forms, all with the same results:
+ *  - streamed (default for rays in pinned memory, 2^17 rays or more, the
+ *    default traversal kernel): the traversal on `stream` starts at once
+ *    and the rays follow in pieces on the handle's copy stream, each warp
+ *    waiting for the piece it takes (see pbrtgpu_intersect_streamed);
+ *    closest hits go straight to device memory or to pinned host memory
+ *    mapped into the device's address space, any-hit answers to host
+ *    memory through one copy.  PBRT_STREAM_IN=0 turns it off;
+ *  - in place (PBRT_HOST_MAPPED=1, pinned buffers): the traversal reads and
+ *    writes the mapped host memory;
+ *  - pipelined (every other host buffer): copies in and out and the
+ *    traversal in PBRT_PIPE_CHUNKS (default 4) pieces on the handle's own
+ *    streams, for 2^19 rays or more, each piece's copies overlapping the
+ *    others' traversal.
+ * The call returns after the work is queued for device buffers and after
+ * completion for host buffers.  `stream` is a cudaStream_t (NULL = legacy
+ * default stream). */
 int pbrtgpu_intersect(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
                       PbrtHit* hits, void* stream);
 
@@ -278,6 +285,23 @@ int pbrtgpu_intersect(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
  * BVH: occluded[i] = 1 if any primitive is hit within [tmin, tmax]. */
 int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
                         uint8_t* occluded, void* stream);
+
+/* Closest hits (hits non-NULL) or any-hit answers (occluded non-NULL),
+ * device buffers only, for rays that arrive while the walk runs: piece k,
+ * rays [k << piece_shift, (k + 1) << piece_shift), may be read once
+ * ready[k] != 0 (ready: device memory, one uint32 per piece).  Set the
+ * flags with copies (cudaMemcpyAsync on another stream) or host writes to
+ * mapped memory, never from a kernel: the walk may hold every SM until the
+ * flags are set.  piece_shift in [5, 31].  Needs the 4-wide persistent walk
+ * with its work counter (the default configuration; PBRT_ERR_UNSUPPORTED
+ * otherwise).  Returns after the walk; a piece whose flag is not set within
+ * 2 s ends the call with PBRT_ERR_TIMEOUT and its rays get no result.  The
+ * streamed form of pbrtgpu_intersect is this call with the library setting
+ * the flags behind its own copies.  No counterpart in the reference. */
+int pbrtgpu_intersect_streamed(const PbrtBVH* bvh, const PbrtRay* rays,
+                               uint32_t n, PbrtHit* hits, uint8_t* occluded,
+                               const uint32_t* ready, uint32_t piece_shift,
+                               void* stream);
 
 /* Traversal kernel choice (process-wide), set by the autotuner.  Every
  * kernel visits the reference's tree in the reference's order, so results

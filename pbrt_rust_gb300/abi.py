@@ -191,6 +191,7 @@ SIGNATURES = {
     "pbrtgpu_bvh_get_primitive_order": (C.c_int, [_P, _U32P, C.c_uint32]),
     "pbrtgpu_intersect": (C.c_int, [_P, _P, C.c_uint32, _P, _P]),
     "pbrtgpu_intersect_p": (C.c_int, [_P, _P, C.c_uint32, _P, _P]),
+    "pbrtgpu_intersect_streamed": (C.c_int, [_P, _P, C.c_uint32, _P, _P, _P, C.c_uint32, _P]),
     "pbrtgpu_set_trace_config": (C.c_int, [C.POINTER(PbrtTraceConfig)]),
     "pbrtgpu_get_trace_config": (C.c_int, [C.POINTER(PbrtTraceConfig)]),
     "pbrtgpu_scene_create": (C.c_int, [C.POINTER(PbrtSceneDesc), C.POINTER(_P)]),

@@ -183,13 +183,14 @@ static int scratch_pool(int dev, cudaMemPool_t* out) {
 // origin when the configuration asks for it (reorder.cu); the permutation
 // lives in stream-ordered scratch released on the same stream.
 static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* d_hits, uint8_t* d_occ,
-                        cudaStream_t s) {
+                        cudaStream_t s, const uint32_t* ready = nullptr, uint32_t piece_shift = 0,
+                        PbrtHit* host_hits = nullptr) {
     const uint32_t* order = nullptr;
     uint32_t* work = nullptr;
     void* scratch = nullptr;
     int st;
-    const bool reorder = trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
-    const bool chunked = trace_chunk() != 0;
+    const bool reorder = !ready && !host_hits && trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
+    const bool chunked = ready || host_hits || trace_chunk() != 0;
     // [256 B: chunk counter, replay flag][permutation scratch]
     cudaMemPool_t pool = nullptr;
     if ((st = scratch_pool(b->device, &pool))) return st;
@@ -221,7 +222,7 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
         order = ord;
     }
     st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, d_hits, d_occ, b->d_status, s, wide_of(b),
-                                  b->host.stack4_bound, -1, order, work, replay),
+                                  b->host.stack4_bound, -1, order, work, replay, ready, piece_shift, host_hits),
                      "trace launch");
     cudaFreeAsync(scratch, s);
     return st;
@@ -230,11 +231,12 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
 // Pinned host memory is mapped into the device's address space (on GB300
 // it is the Grace memory behind NVLink-C2C).  With PBRT_HOST_MAPPED=1 (read
 // at every call) the traversal reads the rays and writes the results there
-// directly, with no staging copies; by default pinned buffers take the copy
-// pipeline below.  Measured with 2^22 heightfield rays in pinned buffers on
-// several GB300 machines: in place 1.60-1.82 ms per call depending on the box
-// (2306-2614 Mrays/s), the copy pipeline 1.74-1.75 ms on every box (2403-2414
-// Mrays/s); the pipeline has the better worst case.  Identical results.
+// directly, with no staging copies; by default pinned buffers take the
+// streamed form (trace_streamed) and other host buffers the copy pipeline
+// below.  Measured with 2^22 heightfield rays in pinned buffers on GB300
+// boxes: in place 1.57-1.99 ms per call depending on the box (its scattered
+// 16-byte stores run at 37 GB/s across the link on some boxes), the copy
+// pipeline 1.68-1.76 ms, the streamed form 1.48 ms.  Identical results.
 static bool host_mapped_enabled() {
     const char* v = getenv("PBRT_HOST_MAPPED");
     return v && v[0] == '1';
@@ -258,6 +260,7 @@ static void* mapped_host_pointer(const void* p) {
 // chunks (one compute stream: 1.82 / 1.87 / 2.04 ms).
 constexpr uint32_t kPipeChunkMin = 1u << 18;
 constexpr uint32_t kPipeChunks = 8;
+constexpr uint32_t kStreamPieces = 64;  // streamed input (trace_streamed): pieces per call at most
 static uint32_t pipe_chunks() {
     static const uint32_t k = [] {
         const char* v = getenv("PBRT_PIPE_CHUNKS");
@@ -265,6 +268,19 @@ static uint32_t pipe_chunks() {
         return (uint32_t)(x < 1 ? 1 : (x > (int)kPipeChunks ? (int)kPipeChunks : x));
     }();
     return k;
+}
+
+// The handle's device-side status after a finished call (cleared when set).
+static int device_status(PbrtBVH* b) {
+    int dev_status = 0, st;
+    if ((st = cuda_status(cudaMemcpy(&dev_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status")))
+        return st;
+    if (dev_status) {
+        cudaMemset(b->d_status, 0, sizeof(int));
+        return set_error(dev_status, dev_status == PBRT_ERR_TIMEOUT ? "streamed rays did not arrive in time"
+                                                                     : "device-side traversal failure");
+    }
+    return PBRT_OK;
 }
 
 // The handle's copy streams and events (created on first use; the caller
@@ -278,7 +294,90 @@ static int pipe_streams(PbrtBVH* b) {
         return st;
     for (cudaEvent_t& e : b->pipe_ev)
         if ((st = cuda_status(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate"))) return st;
+    if ((st = cuda_status(cudaMalloc(&b->d_ready, kStreamPieces * sizeof(uint32_t)), "cudaMalloc")) ||
+        (st = cuda_status(cudaHostAlloc(&b->h_one, sizeof(uint32_t), cudaHostAllocDefault), "cudaHostAlloc")))
+        return st;
+    *b->h_one = 1u;
     return PBRT_OK;
+}
+
+// Streamed host input.  Rays in pinned host memory, results in device
+// memory or (closest hits) in pinned host memory mapped into the device's
+// address space: the traversal is launched first, then the rays follow in
+// pieces of 2^shift rays (at most kStreamPieces, at least 2^kStreamShiftMin
+// rays each) on the copy stream, each piece's copy followed by a 4-byte copy
+// that sets the piece's flag.  The kernel's warps take rays in order and
+// wait (bounded) for the piece they need, so the traversal starts after the
+// first piece instead of after every copy, and one launch replaces the
+// copy pipeline's per-chunk launches.  Closest hits for host memory are
+// staged on the device and written out by the walk itself, each chunk of
+// rays in coalesced rows once its last ray is done (HOSTOUT in trace.cu);
+// any-hit answers for host memory go through the staging buffer and one
+// copy of n bytes.  PBRT_STREAM_IN=0 (read at every call) takes the copy
+// pipeline instead.  Measured on GB300 with 2^22 heightfield rays (the walk
+// alone: 1.30 ms): closest hits 1.48 ms per call (pipeline 1.68 ms), any hit
+// 1.22 ms (1.40 ms); with device outputs 1.39 ms.  Over the pipeline's
+// per-piece launches it saves the tails each launch leaves (a 2^22-ray pass
+// in four launches spent 1.50 ms in kernels against 1.30 ms in one).
+constexpr uint32_t kStreamShiftMin = 16;
+static bool stream_in_enabled() {
+    const char* v = getenv("PBRT_STREAM_IN");
+    return !(v && v[0] == '0');
+}
+// The caller holds stage_mu.  `hits`: the closest hits' destination, device
+// memory (`out_dev`) or mapped pinned host memory; `occ`: the any-hit
+// destination, device memory (`out_dev`) or any host memory.
+static int trace_streamed(PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit* hits, uint8_t* occ, bool out_dev,
+                          cudaStream_t s) {
+    int st;
+    if ((st = pipe_streams(b)) || (st = b->stage_in.reserve((size_t)n * sizeof(PbrtRay)))) return st;
+    uint8_t* d_occ = occ;
+    PbrtHit* d_hits = hits;
+    PbrtHit* host_hits = nullptr;
+    if (!out_dev) {
+        if ((st = b->stage_out.reserve(hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n))) return st;
+        if (hits) {
+            host_hits = hits;
+            d_hits = static_cast<PbrtHit*>(b->stage_out.p);
+        } else {
+            d_occ = static_cast<uint8_t*>(b->stage_out.p);
+        }
+    }
+    uint32_t shift = kStreamShiftMin;
+    while (((uint64_t)kStreamPieces << shift) < n) ++shift;
+    const uint32_t pieces = (uint32_t)(((uint64_t)n + (1ull << shift) - 1) >> shift);
+    PbrtRay* d_rays = static_cast<PbrtRay*>(b->stage_in.p);
+    // the flags are cleared before the copy stream may set them
+    if ((st = cuda_status(cudaMemsetAsync(b->d_ready, 0, kStreamPieces * sizeof(uint32_t), s), "cudaMemsetAsync")) ||
+        (st = cuda_status(cudaEventRecord(b->pipe_ev[0], s), "cudaEventRecord")) ||
+        (st = cuda_status(cudaStreamWaitEvent(b->pipe_in, b->pipe_ev[0], 0), "cudaStreamWaitEvent")))
+        return st;
+    const int launch_st = launch_batch(b, d_rays, n, d_hits, d_occ, s, b->d_ready, shift, host_hits);
+    // the copies are queued whatever the launch did: a walk that did start
+    // waits for them
+    int copy_st = PBRT_OK;
+    for (uint32_t k = 0; k < pieces && !copy_st; ++k) {
+        const uint64_t lo = (uint64_t)k << shift;
+        const uint64_t cnt = std::min<uint64_t>((uint64_t)n - lo, 1ull << shift);
+        copy_st = cuda_status(cudaMemcpyAsync(d_rays + lo, rays + lo, cnt * sizeof(PbrtRay), cudaMemcpyHostToDevice,
+                                              b->pipe_in),
+                              "cudaMemcpyAsync H2D");
+        if (!copy_st)
+            copy_st = cuda_status(cudaMemcpyAsync(b->d_ready + k, b->h_one, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                                  b->pipe_in),
+                                  "cudaMemcpyAsync H2D");
+    }
+    if (!launch_st && !copy_st && occ && d_occ != occ)
+        copy_st = cuda_status(cudaMemcpyAsync(occ, d_occ, n, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
+    // a walk whose pieces never come ends by itself (PBRT_ERR_TIMEOUT)
+    const int sync_st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    const int sync_in = cuda_status(cudaStreamSynchronize(b->pipe_in), "cudaStreamSynchronize");
+    if (launch_st || copy_st) {
+        const int first = launch_st ? launch_st : copy_st;
+        device_status(b);  // clears a timeout the failed copies caused
+        return first;
+    }
+    return sync_st ? sync_st : sync_in;
 }
 
 // Runs closest/any hit for host or device buffers.
@@ -296,6 +395,19 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
     size_t out_bytes = hits ? (size_t)n * sizeof(PbrtHit) : (size_t)n;
     bool dr = is_device_pointer(rays), dout = is_device_pointer(out);
     if (dr && dout) return launch_batch(b, rays, n, hits, occ, s);
+    if (dr && hits && stream_in_enabled() && !host_mapped_enabled() && n >= (2u << kStreamShiftMin) &&
+        trace_streams(b->dev, wide_of(b), b->host.stack4_bound, n)) {
+        // device rays, closest hits for mapped pinned host memory: the walk
+        // writes them out chunk by chunk from a staging array
+        if (PbrtHit* mh = static_cast<PbrtHit*>(mapped_host_pointer(hits))) {
+            std::lock_guard<std::mutex> lk(b->stage_mu);
+            if ((st = b->stage_out.reserve((size_t)n * sizeof(PbrtHit))) ||
+                (st = launch_batch(b, rays, n, static_cast<PbrtHit*>(b->stage_out.p), nullptr, s, nullptr, 0, mh)) ||
+                (st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize")))
+                return st;
+            return device_status(b);
+        }
+    }
     if (host_mapped_enabled()) {
         const void* mr = dr ? (const void*)rays : mapped_host_pointer(rays);
         void* mo = dout ? out : mapped_host_pointer(out);
@@ -307,6 +419,14 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
         }
     }
     std::lock_guard<std::mutex> lk(b->stage_mu);
+    if (!dr && n >= (2u << kStreamShiftMin) && stream_in_enabled() && mapped_host_pointer(rays) &&
+        trace_streams(b->dev, wide_of(b), b->host.stack4_bound, n)) {
+        PbrtHit* d_hits = hits && !dout ? static_cast<PbrtHit*>(mapped_host_pointer(hits)) : hits;
+        if (!hits || d_hits) {
+            if ((st = trace_streamed(b, rays, n, d_hits, occ, dout, s))) return st;
+            return device_status(b);
+        }
+    }
     const PbrtRay* d_rays = rays;
     if (!dr) {
         if ((st = b->stage_in.reserve((size_t)n * sizeof(PbrtRay)))) return st;
@@ -380,14 +500,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
             return st;
         if ((st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"))) return st;
     }
-    int dev_status = 0;
-    if ((st = cuda_status(cudaMemcpy(&dev_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status")))
-        return st;
-    if (dev_status) {
-        cudaMemset(b->d_status, 0, sizeof(int));
-        return set_error(dev_status, "device-side traversal failure");
-    }
-    return PBRT_OK;
+    return device_status(b);
 }
 
 }  // namespace pbrt
@@ -398,6 +511,8 @@ PbrtBVH::~PbrtBVH() {
     if (pipe_in) cudaStreamDestroy(pipe_in);
     if (pipe_out) cudaStreamDestroy(pipe_out);
     if (pipe_k) cudaStreamDestroy(pipe_k);
+    if (d_ready) cudaFree(d_ready);
+    if (h_one) cudaFreeHost(h_one);
     for (void* p : d_inst_bufs) cudaFree(p);
     if (d_insts) cudaFree(d_insts);
     if (d_pairs) cudaFree(d_pairs);
@@ -573,6 +688,29 @@ int pbrtgpu_intersect(const PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit
 int pbrtgpu_intersect_p(const PbrtBVH* b, const PbrtRay* rays, uint32_t n, uint8_t* occluded, void* stream) {
     if (!occluded && n) return set_error(PBRT_ERR_INVALID_ARGUMENT, "occluded is NULL");
     return trace_call(b, rays, n, nullptr, occluded, stream);
+}
+
+int pbrtgpu_intersect_streamed(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHit* hits, uint8_t* occluded,
+                               const uint32_t* ready, uint32_t piece_shift, void* stream) {
+    using namespace pbrt;
+    PbrtBVH* b = const_cast<PbrtBVH*>(cb);
+    if (!b) return set_error(PBRT_ERR_INVALID_ARGUMENT, "bvh is NULL");
+    if (n == 0) return PBRT_OK;
+    if (!rays || !ready || (!hits) == (!occluded))
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "rays/ready NULL or not exactly one of hits/occluded");
+    if (piece_shift < 5 || piece_shift > 31) return set_error(PBRT_ERR_INVALID_ARGUMENT, "piece_shift not in [5, 31]");
+    void* out = hits ? (void*)hits : (void*)occluded;
+    if (!is_device_pointer(rays) || !is_device_pointer(out) || !is_device_pointer(ready))
+        return set_error(PBRT_ERR_INVALID_ARGUMENT, "rays, results and flags must be device memory");
+    int st;
+    if (!b->uploaded && (st = bvh_upload(b))) return st;
+    DeviceGuard g(b->device);
+    if (!trace_streams(b->dev, wide_of(b), b->host.stack4_bound, n))
+        return set_error(PBRT_ERR_UNSUPPORTED, "streamed rays need the 4-wide persistent walk with a work counter");
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((st = launch_batch(b, rays, n, hits, occluded, s, ready, piece_shift))) return st;
+    if ((st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"))) return st;
+    return device_status(b);
 }
 
 }  // extern "C"

@@ -56,6 +56,8 @@ struct PbrtBVH {
     pbrt::DeviceBuf stage_in, stage_out;
     cudaStream_t pipe_in = nullptr, pipe_out = nullptr, pipe_k = nullptr;  // pipelined host-buffer calls
     cudaEvent_t pipe_ev[17] = {};                        // entry + 2 per chunk (8 chunks)
+    uint32_t* d_ready = nullptr;  // streamed input: a flag per piece
+    uint32_t* h_one = nullptr;    // pinned host word holding 1, copied into a flag
     ~PbrtBVH();
 };
 

@@ -3,6 +3,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "../../include/pbrt_gpu.h"
 #include "kernels.h"
@@ -162,24 +163,91 @@ __global__ void __launch_bounds__(128) k_trace4(const __grid_constant__ DevBVH4 
     }
 }
 
+// Streamed input: the rays arrive in pieces of 2^piece_shift rays while the
+// traversal already runs, and ready[k] turns non-zero once piece k has
+// landed (the copy stream writes it with a 4-byte copy queued behind the
+// piece's own copy).  %globaltimer is the GPU's nanosecond clock.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// A piece's copy takes well under a millisecond; two seconds without its
+// flag means the copies never ran, and the warp gives up instead of hanging
+// (at once when another warp already gave up: *status holds the timeout).
+constexpr uint64_t kPieceWaitNs = 2000000000ull;
+__device__ __noinline__ bool wait_piece(const uint32_t* ready, uint32_t k, const int* status) {
+    if (ld_acquire_u32(ready + k)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        __nanosleep(256);
+        if (ld_acquire_u32(ready + k)) return true;
+        if (global_ns() - t0 > kPieceWaitNs ||
+            ld_acquire_u32(reinterpret_cast<const uint32_t*>(status)) == (uint32_t)PBRT_ERR_TIMEOUT)
+            return false;
+    }
+}
+
 // 4-wide traversal with persistent warps refilling idle lanes (see
 // k_trace_persistent).  Without `work`, warp w owns rays
 // [w * per_warp, (w + 1) * per_warp); with it, warps take chunks of
 // per_warp rays from the shared counter *work (zero at launch) whenever
 // their chunk is used up, so warps that drew short rays take more of them
-// and no warp is left with a long tail.
-template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
+// and no warp is left with a long tail.  With `ready` (streamed input; only
+// with `work`, which hands out chunks in ray order) a warp that takes a
+// chunk first waits for the piece holding its last ray, and reads rays
+// through L2 (they are written while the kernel runs); a wait that runs out
+// sets PBRT_ERR_TIMEOUT and the warp drops its chunk.
+//
+// HOSTOUT (closest hits, with `work`): `hits` is a device staging array and
+// `host_hits` the caller's pinned host memory mapped into the device's
+// address space.  Scattered 16-byte stores across NVLink-C2C run at a fifth
+// of its bandwidth (measured on GB300: 37 against 191 GB/s for 1 KiB runs),
+// so each warp counts its chunks' finished rays in a ring of 4 slots in
+// shared memory and copies a chunk's hits from the staging array to the
+// host in coalesced rows once its last ray is done; a warp takes a new
+// chunk only when a slot is free (always the case once all its lanes are
+// idle).  The copies spread over the walk, sharing the link with the
+// streamed input.
+constexpr uint32_t kRingWords = 10 + 32;  // HOSTOUT: per warp, see k_trace4_persistent
+// HOSTOUT's copy of finished chunks (ring[9]: one bit per slot) from the
+// staging array to the host, one row of the warp's lanes at a time; out of
+// line, so that the walk keeps its registers.
+static __device__ __noinline__ void write_out_chunks(uint32_t* ring, const float4* hits, float4* host_hits, uint32_t n,
+                                                     uint32_t per_warp) {
+    const unsigned lane = threadIdx.x & 31u;
+    uint32_t dm = ring[9];
+    __syncwarp();
+    if (lane == 0) ring[9] = 0u;
+    while (dm) {
+        const uint32_t j = (uint32_t)(__ffs(dm) - 1);
+        dm &= dm - 1u;
+        const uint32_t base = ring[4 + j];
+        const uint32_t cnt = min(per_warp, n - base);
+        for (uint32_t k = lane; k < cnt; k += 32u) host_hits[base + k] = __ldcg(hits + base + k);
+    }
+}
+template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false, bool HOSTOUT = false>
 __global__ void __launch_bounds__(128, MINB)
     k_trace4_persistent(const __grid_constant__ DevBVH4 bvh, const float4* __restrict__ rays, uint32_t n,
                         const uint32_t* __restrict__ order,
                         float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status,
                         uint32_t per_warp, uint32_t refill, uint32_t* __restrict__ work,
-                        uint32_t* __restrict__ replay) {
+                        uint32_t* __restrict__ replay, const uint32_t* __restrict__ ready, uint32_t piece_shift,
+                        float4* __restrict__ host_hits) {
+    static_assert(!(HOSTOUT && ANY), "host write-out is for closest hits");
     extern __shared__ uint2 smem_stack[];
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint64_t next = work ? 0 : warp * per_warp;
-    uint64_t end = work ? 0 : ((next + per_warp < (uint64_t)n) ? next + per_warp : (uint64_t)n);
+    // ray positions (32 bits suffice for the counter mode, n <= 0xF0000000)
+    using Pos = typename std::conditional<HOSTOUT, uint32_t, uint64_t>::type;
+    Pos next = work ? 0 : (Pos)(warp * per_warp);
+    Pos end = work ? 0 : (Pos)((warp * per_warp + per_warp < (uint64_t)n) ? warp * per_warp + per_warp : (uint64_t)n);
     bool more = work != nullptr;  // the shared counter may still hold rays
     const uint32_t kNone = 0xffffffffu;
     uint32_t ray = kNone;
@@ -187,33 +255,102 @@ __global__ void __launch_bounds__(128, MINB)
     DRay r;
     Traversal4<SMAX, OVF, INST> T;
     T.bind(smem_stack, threadIdx.x, blockDim.x);
+    // HOSTOUT: this warp's ring in shared memory: rays left in slot j at
+    // ring[j], the slot's first ray at ring[4 + j], the slot of the chunk
+    // being handed out at ring[8], the slots whose last ray finished (a bit
+    // each) at ring[9], then each lane's slot at ring[10 + lane].  Nothing of
+    // it lives in registers, which the walk needs.
+    auto ring_of = [&]() -> uint32_t* {
+        uint32_t tid;  // read afresh at each use: the address is not kept in a register across the walk
+        asm volatile("mov.u32 %0, %%tid.x;" : "=r"(tid));
+        return reinterpret_cast<uint32_t*>(smem_stack + SMAX * blockDim.x) + (tid >> 5) * kRingWords;
+    };
+    if constexpr (HOSTOUT) {
+        if (lane < 10) ring_of()[lane] = 0u;
+        __syncwarp();
+    }
+    auto put = [&](float4 h) {
+        hits[ray] = h;
+        if constexpr (HOSTOUT) {
+            uint32_t* ring = ring_of();
+            const uint32_t j = ring[10 + lane];
+            if (atomicSub(ring + j, 1u) == 1u) atomicOr(ring + 9, 1u << j);
+        }
+    };
+    // HOSTOUT: the chunks whose last ray finished go out to the host.  Done
+    // when the warp takes its next chunk (which needs a slot) and at the
+    // end, not at every step of the walk.
+    auto write_out = [&]() {
+        if constexpr (HOSTOUT) {
+            __syncwarp();  // the chunks' staged hits and the ring are visible to every lane
+            uint32_t* ring = ring_of();
+            if (ring[9]) write_out_chunks(ring, hits, host_hits, n, per_warp);
+        }
+    };
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, ray == kNone);
         unsigned nidle = __popc(idle);
         if (more && next >= end && nidle >= refill) {  // warp-uniform
-            uint32_t base = 0;
-            if (lane == 0) base = atomicAdd(work, per_warp);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base < n) {
-                next = base;
-                end = (uint64_t)base + per_warp < (uint64_t)n ? (uint64_t)base + per_warp : (uint64_t)n;
-            } else {
-                more = false;
+            int fs = 0;  // HOSTOUT: a free slot for the next chunk, -1 when none is
+            if constexpr (HOSTOUT) {
+                write_out();  // frees the slots of finished chunks
+                __syncwarp();
+                const uint32_t* ring = ring_of();
+                fs = -1;
+                for (int j = 3; j >= 0; --j)
+                    if (ring[j] == 0u) fs = j;
+            }
+            if (fs >= 0) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(work, per_warp);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base < n) {
+                    next = base;
+                    end = (Pos)((uint64_t)base + per_warp < (uint64_t)n ? (uint64_t)base + per_warp : (uint64_t)n);
+                    if (ready) {  // streamed input: the chunk's rays must have landed
+                        int ok = 1;
+                        if (lane == 0)
+                            ok = wait_piece(ready, (uint32_t)((end - 1) >> piece_shift), status) ? 1 : 0;
+                        if (!__shfl_sync(0xffffffffu, ok, 0)) {
+                            if (lane == 0) atomicMax(status, PBRT_ERR_TIMEOUT);
+                            next = end;
+                            more = false;
+                        }
+                    }
+                    if constexpr (HOSTOUT) {
+                        if (next < end) {
+                            if (lane == 0) {
+                                uint32_t* ring = ring_of();
+                                ring[fs] = (uint32_t)(end - next);
+                                ring[4 + fs] = base;
+                                ring[8] = (uint32_t)fs;
+                            }
+                            __syncwarp();
+                        }
+                    }
+                } else {
+                    more = false;
+                }
             }
         }
         const bool tail = !more && next + nidle >= end;
         if (next < end && nidle >= (tail ? 1u : refill)) {
             if (ray == kNone) {
-                uint64_t my = next + __popc(idle & ((1u << lane) - 1u));
+                const Pos my = next + __popc(idle & ((1u << lane) - 1u));
                 if (my < end) {
                     ray = order ? __ldg(order + my) : (uint32_t)my;
-                    r = make_dray(__ldg(rays + 2 * (size_t)ray), __ldg(rays + 2 * (size_t)ray + 1));
+                    if constexpr (HOSTOUT) {
+                        uint32_t* ring = ring_of();
+                        ring[10 + lane] = ring[8];
+                    }
+                    const float4* rp = rays + 2 * (size_t)ray;
+                    r = ready ? make_dray(__ldcg(rp), __ldcg(rp + 1)) : make_dray(__ldg(rp), __ldg(rp + 1));
                     bool live = T.start(bvh, r);
                     if (!live) {
                         if (ANY)
                             occ[ray] = 0;
                         else
-                            hits[ray] = make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f);
+                            put(make_float4(__int_as_float(-1), 0.0f, 0.0f, 0.0f));
                         ray = kNone;
                     }
                 }
@@ -231,15 +368,16 @@ __global__ void __launch_bounds__(128, MINB)
                 occ[ray] = T.found ? 1 : 0;
             } else {
                 if (T.nan_hit) {
-                    hits[ray] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+                    put(make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f));
                     *replay = 1u;
                 } else {
-                    hits[ray] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+                    put(make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2));
                 }
             }
             ray = kNone;
         }
     }
+    write_out();
     if (overflow) atomicMax(status, 6);
 }
 
@@ -394,10 +532,13 @@ static void read_variant() {
 // Rewrites the closest hits marked kReplayMark by the EXACT walk (see
 // Traversal in trace.cuh); returns at once when no ray of the launch was
 // marked, so a launch without NaN-distance hits pays one empty kernel.
+// `host_hits` (may be null): a second copy of the hits that the rewritten
+// ones also go to (the host memory of a write-out walk).
 template <int SMAX, int OVF, bool INST>
 __global__ void __launch_bounds__(128) k_replay4(const __grid_constant__ DevBVH4 bvh, const float4* __restrict__ rays,
                                                  uint32_t n, float4* __restrict__ hits,
-                                                 const uint32_t* __restrict__ replay, int* __restrict__ status) {
+                                                 const uint32_t* __restrict__ replay, int* __restrict__ status,
+                                                 float4* __restrict__ host_hits) {
     extern __shared__ uint2 smem_stack[];
     if (*(const volatile uint32_t*)replay == 0u) return;
     Traversal4<SMAX, OVF, INST, true, true> T;
@@ -411,6 +552,7 @@ __global__ void __launch_bounds__(128) k_replay4(const __grid_constant__ DevBVH4
         }
         if (T.overflow) atomicMax(status, 6);
         hits[i] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        if (host_hits) host_hits[i] = hits[i];
     }
 }
 
@@ -430,15 +572,19 @@ __global__ void __launch_bounds__(128) k_replay2(const __grid_constant__ DevBVH 
     }
 }
 
-template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false>
+// `host_hits` (closest hits, with `work`): the HOSTOUT walk, `h4` its
+// staging array.
+template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false, bool HOSTOUT = false>
 static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                           float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
-                                          uint32_t* work, uint32_t* replay) {
+                                          uint32_t* work, uint32_t* replay, const uint32_t* ready = nullptr,
+                                          uint32_t piece_shift = 0, float4* host_hits = nullptr) {
     const int block = 128;
-    const size_t smem = (size_t)SMAX * sizeof(uint2) * block;
+    // HOSTOUT: each warp's ring after the stacks
+    const size_t smem = (size_t)SMAX * sizeof(uint2) * block + (HOSTOUT ? (block / 32) * kRingWords * sizeof(uint32_t) : 0);
     static ShapeCache bps_cache;
     const int sms = device_sms();
-    const int bps = resident_blocks(bps_cache, k_trace4_persistent<SMAX, OVF, ANY, MINB, INST>, block, smem);
+    const int bps = resident_blocks(bps_cache, k_trace4_persistent<SMAX, OVF, ANY, MINB, INST, HOSTOUT>, block, smem);
     uint64_t warps = (uint64_t)sms * bps * (block / 32);
     uint32_t per_warp = (uint32_t)((n + warps - 1) / warps);
     if (per_warp < 32) per_warp = 32;
@@ -448,15 +594,17 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
         uint64_t chunks = (n + g_chunk - 1) / g_chunk;
         uint64_t w = chunks < warps ? chunks : warps;
         unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
-        k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(
-            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work, replay);
+        k_trace4_persistent<SMAX, OVF, ANY, MINB, INST, HOSTOUT><<<grid, block, smem, stream>>>(
+            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work, replay, ready, piece_shift, host_hits);
         return cudaGetLastError();
     }
+    // fixed per-warp ranges would read rays out of order and have no chunks
+    // to write out: no streamed input, no write-out
+    if (ready || HOSTOUT) return cudaErrorInvalidValue;
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
-    k_trace4_persistent<SMAX, OVF, ANY, MINB, INST><<<grid, block, smem, stream>>>(bvh, r4, n, order, h4, occ,
-                                                                                  d_status, per_warp, g_refill,
-                                                                                  nullptr, replay);
+    k_trace4_persistent<SMAX, OVF, ANY, MINB, INST, HOSTOUT><<<grid, block, smem, stream>>>(
+        bvh, r4, n, order, h4, occ, d_status, per_warp, g_refill, nullptr, replay, nullptr, 0, nullptr);
     return cudaGetLastError();
 }
 
@@ -683,14 +831,74 @@ static cudaError_t launch_main(const DevBVH& bvh, uint32_t depth, const PbrtRay*
     return cudaGetLastError();
 }
 
+bool trace_streams(const DevBVH& bvh, const DevBVH4* wide, uint32_t wide_bound, uint32_t n) {
+    read_variant();
+    if (!wide || !wide_stack_variant(wide_bound) || !g_chunk || g_reorder || n > 0xF0000000u) return false;
+    // scenes with instances always take the 4-wide persistent walk
+    return bvh.insts != nullptr || (g_kernel_variant == kVariantWidePersistent && g_min_blocks == 0);
+}
+
+// The launch of a streamed-input or write-out call: the 4-wide persistent
+// walk with its shared counter (the only kernel that takes rays in order).
+static cudaError_t launch_streamed(const DevBVH& bvh, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
+                                   uint8_t* occ, int* d_status, cudaStream_t stream, const DevBVH4* wide,
+                                   uint32_t wide_bound, uint32_t* work, uint32_t* replay, const uint32_t* ready,
+                                   uint32_t shift, PbrtHit* host_hits) {
+    if (!work || !trace_streams(bvh, wide, wide_bound, n) || (host_hits && occ)) return cudaErrorInvalidValue;
+    const float4* r4 = reinterpret_cast<const float4*>(rays);
+    float4* h4 = reinterpret_cast<float4*>(hits);
+    const bool any = occ != nullptr, inst = bvh.insts != nullptr;
+    if (host_hits) {
+        float4* hh = reinterpret_cast<float4*>(host_hits);
+        if (wide_stack_variant(wide_bound) == 64)
+            return inst ? launch_wide_persistent<16, 48, false, 0, true, true>(*wide, r4, n, nullptr, h4, nullptr,
+                                                                              d_status, stream, work, replay, ready,
+                                                                              shift, hh)
+                        : launch_wide_persistent<16, 48, false, 0, false, true>(*wide, r4, n, nullptr, h4, nullptr,
+                                                                               d_status, stream, work, replay, ready,
+                                                                               shift, hh);
+        return inst ? launch_wide_persistent<16, 240, false, 0, true, true>(*wide, r4, n, nullptr, h4, nullptr,
+                                                                           d_status, stream, work, replay, ready,
+                                                                           shift, hh)
+                    : launch_wide_persistent<16, 240, false, 0, false, true>(*wide, r4, n, nullptr, h4, nullptr,
+                                                                            d_status, stream, work, replay, ready,
+                                                                            shift, hh);
+    }
+    if (wide_stack_variant(wide_bound) == 64) {
+        if (inst)
+            return any ? launch_wide_persistent<16, 48, true, 0, true>(*wide, r4, n, nullptr, nullptr, occ, d_status,
+                                                                       stream, work, replay, ready, shift)
+                       : launch_wide_persistent<16, 48, false, 0, true>(*wide, r4, n, nullptr, h4, nullptr, d_status,
+                                                                        stream, work, replay, ready, shift);
+        return any ? launch_wide_persistent<16, 48, true, 0>(*wide, r4, n, nullptr, nullptr, occ, d_status, stream,
+                                                             work, replay, ready, shift)
+                   : launch_wide_persistent<16, 48, false, 0>(*wide, r4, n, nullptr, h4, nullptr, d_status, stream,
+                                                              work, replay, ready, shift);
+    }
+    if (inst)
+        return any ? launch_wide_persistent<16, 240, true, 0, true>(*wide, r4, n, nullptr, nullptr, occ, d_status,
+                                                                    stream, work, replay, ready, shift)
+                   : launch_wide_persistent<16, 240, false, 0, true>(*wide, r4, n, nullptr, h4, nullptr, d_status,
+                                                                     stream, work, replay, ready, shift);
+    return any ? launch_wide_persistent<16, 240, true, 0>(*wide, r4, n, nullptr, nullptr, occ, d_status, stream,
+                                                          work, replay, ready, shift)
+               : launch_wide_persistent<16, 240, false, 0>(*wide, r4, n, nullptr, h4, nullptr, d_status, stream, work,
+                                                           replay, ready, shift);
+}
+
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
-                         uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work, uint32_t* replay) {
+                         uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work, uint32_t* replay,
+                         const uint32_t* ready, uint32_t piece_shift, PbrtHit* host_hits) {
     if (n == 0) return cudaSuccess;
     if (!occluded && !replay) return cudaErrorInvalidValue;
     read_variant();
-    cudaError_t e = launch_main(bvh, depth, rays, n, hits, occluded, d_status, stream, wide, wide_bound, kernel, order,
-                                work, replay);
+    if ((ready || host_hits) && order) return cudaErrorInvalidValue;
+    cudaError_t e = ready || host_hits
+                        ? launch_streamed(bvh, rays, n, hits, occluded, d_status, stream, wide, wide_bound, work,
+                                          replay, ready, piece_shift, host_hits)
+                        : launch_main(bvh, depth, rays, n, hits, occluded, d_status, stream, wide, wide_bound, kernel,
+                                      order, work, replay);
     if (e != cudaSuccess || occluded) return e;
     // the replay pass of closest hits (one empty launch unless a ray was marked)
     const unsigned grid = (unsigned)(device_sms() * 4);
@@ -699,12 +907,13 @@ cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays,
     const bool inst = bvh.insts != nullptr;
     const int v = wide ? wide_stack_variant(wide_bound) : 0;
     const size_t smem = 16 * sizeof(uint2) * 128;
+    float4* hh = reinterpret_cast<float4*>(host_hits);
     if (v == 64)
-        inst ? k_replay4<16, 48, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status)
-             : k_replay4<16, 48, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status);
+        inst ? k_replay4<16, 48, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status, hh)
+             : k_replay4<16, 48, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status, hh);
     else if (v == 256)
-        inst ? k_replay4<16, 240, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status)
-             : k_replay4<16, 240, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status);
+        inst ? k_replay4<16, 240, true><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status, hh)
+             : k_replay4<16, 240, false><<<grid, 128, smem, stream>>>(*wide, r4, n, h4, replay, d_status, hh);
     else if (trace_stack_for_depth(depth) == 64)
         inst ? k_replay2<64, true><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status)
              : k_replay2<64, false><<<grid, 128, 0, stream>>>(bvh, r4, n, h4, replay, d_status);

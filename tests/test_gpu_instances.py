@@ -27,6 +27,27 @@ def test_instance_queries_are_bit_exact(oracle, device_build):
     assert np.array_equal(g.intersect_p(rays), o.intersect_p(rays))
 
 
+def test_instance_queries_from_pinned_host_memory(oracle):
+    """Pinned host rays on a tree with instances take the streamed form
+    (the instanced walk waiting for ray pieces, closest hits written out
+    chunk by chunk): the answers equal the oracle's bit for bit."""
+    import torch
+    prims, _, _, _, _ = G.instanced_forest(n_instances=24, tris_per_tree=500, seed=12)
+    n = (1 << 17) + 999
+    rays = G.rays_toward_center(G.PCG32(6), n, radius=14.0, target=4.0)
+    g = GpuBVHAccel(prims, 4, "sah")
+    o = oracle.OracleBVH(prims, 4, "sah")
+    want = o.intersect(rays)
+    assert (want["prim"] >= 0).sum() > 10000
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    out = torch.full((n, 4), 7.0, dtype=torch.float32).pin_memory()
+    g.intersect(pinned, out=out)
+    assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    occ = torch.full((n,), 9, dtype=torch.uint8).pin_memory()
+    g.intersect_p(pinned, out=occ)
+    assert np.array_equal(occ.numpy(), o.intersect_p(rays))
+
+
 def test_instance_ids_cover_every_definition_primitive(oracle):
     """Hits land inside many instances and on primitives of both
     definitions; ids stay below the counted-out total."""

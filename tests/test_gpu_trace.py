@@ -421,10 +421,13 @@ def test_pipelined_host_buffers_equal_device_buffers():
 
 
 @pytest.mark.gpu
-def test_pinned_host_buffers_in_place_and_staged(monkeypatch):
-    """Pinned host buffers are staged through device copies by default and
-    read and written in place by the traversal (mapped host memory) with
-    PBRT_HOST_MAPPED=1.  Both, and a pinned/device mix, give the
+@pytest.mark.parametrize("form", ["streamed", "in_place", "pipelined"])
+def test_pinned_host_buffers_every_form(monkeypatch, form):
+    """Pinned host rays take the streamed form by default (the traversal
+    starts at once, the rays follow in pieces it waits for), are read and
+    written in place with PBRT_HOST_MAPPED=1 and go through the copy
+    pipeline with PBRT_STREAM_IN=0.  Every form, with pinned, pageable and
+    device outputs and a ray count that fills no whole piece, gives the
     device-buffer results bit for bit."""
     torch = _torch()
     prims, _ = G.ray_soup(4096, 1, seed=5)
@@ -433,15 +436,106 @@ def test_pinned_host_buffers_in_place_and_staged(monkeypatch):
     rays = G.incoherent_rays(G.PCG32(37), (1 << 19) + 777, lo, hi)
     want, want_any = dev_hits(g, rays), dev_any(g, rays)
     assert (want["prim"] >= 0).sum() > 5000
+    monkeypatch.setenv("PBRT_HOST_MAPPED", "1" if form == "in_place" else "0")
+    monkeypatch.setenv("PBRT_STREAM_IN", "0" if form == "pipelined" else "1")
     pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
-    for mode in ("1", "0"):
-        monkeypatch.setenv("PBRT_HOST_MAPPED", mode)
+    for rep in range(2):  # the second call reuses the handle's staging and flags
         out = torch.full((len(rays), 4), 7.0, dtype=torch.float32).pin_memory()
         g.intersect(pinned, out=out)
-        assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1)), mode
+        assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1)), rep
         occ = torch.full((len(rays),), 9, dtype=torch.uint8).pin_memory()
         g.intersect_p(pinned, out=occ)
-        assert np.array_equal(occ.numpy(), want_any), mode
-        dout = torch.full((len(rays), 4), 7.0, dtype=torch.float32, device="cuda")
-        g.intersect(pinned, out=dout)
-        assert np.array_equal(dout.cpu().numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1)), mode
+        assert np.array_equal(occ.numpy(), want_any), rep
+    dout = torch.full((len(rays), 4), 7.0, dtype=torch.float32, device="cuda")
+    g.intersect(pinned, out=dout)
+    assert np.array_equal(dout.cpu().numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    docc = torch.full((len(rays),), 9, dtype=torch.uint8, device="cuda")
+    g.intersect_p(pinned, out=docc)
+    assert np.array_equal(docc.cpu().numpy(), want_any)
+    hout = torch.full((len(rays), 4), 7.0, dtype=torch.float32).pin_memory()  # device rays, host hits
+    g.intersect(to_dev(rays), out=hout)
+    assert np.array_equal(hout.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    pout = torch.full((len(rays), 4), 7.0, dtype=torch.float32)  # pageable
+    g.intersect(pinned, out=pout)
+    assert np.array_equal(pout.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    pocc = torch.full((len(rays),), 9, dtype=torch.uint8)
+    g.intersect_p(pinned, out=pocc)
+    assert np.array_equal(pocc.numpy(), want_any)
+
+
+def _streamed(bvh, rays_d, out_d, ready, shift, any_hit, stream):
+    import ctypes as C
+    lib = abi.load()
+    hits = None if any_hit else C.c_void_p(out_d.data_ptr())
+    occ = C.c_void_p(out_d.data_ptr()) if any_hit else None
+    return lib.pbrtgpu_intersect_streamed(bvh._h, C.c_void_p(rays_d.data_ptr()), rays_d.shape[0], hits, occ,
+                                          C.c_void_p(ready.data_ptr()), shift, C.c_void_p(stream.cuda_stream))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("any_hit", [False, True])
+def test_streamed_rays_arriving_during_the_walk(any_hit):
+    """pbrtgpu_intersect_streamed: the rays and the piece flags are copied
+    on another stream that starts with the walk, so warps wait for pieces
+    that are still in flight; the results equal the device-buffer call."""
+    torch = _torch()
+    prims, _ = G.ray_soup(4096, 1, seed=6)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    n, shift = (1 << 18) + 4321, 14
+    rays = G.incoherent_rays(G.PCG32(41), n, lo, hi)
+    want = dev_any(g, rays) if any_hit else dev_hits(g, rays).view(np.uint32).reshape(-1, 4)
+    pieces = (n + (1 << shift) - 1) >> shift
+    host = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    ones = torch.ones(pieces, dtype=torch.int32).pin_memory()
+    s, side = torch.cuda.Stream(), torch.cuda.Stream()
+    for rep in range(2):
+        rays_d = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+        ready = torch.zeros(pieces, dtype=torch.int32, device="cuda")
+        out = (torch.full((n,), 9, dtype=torch.uint8, device="cuda") if any_hit
+               else torch.full((n, 4), 7.0, dtype=torch.float32, device="cuda"))
+        torch.cuda.synchronize()
+        start = torch.cuda.Event()
+        start.record(s)
+        side.wait_event(start)
+        with torch.cuda.stream(side):
+            for k in range(pieces):
+                lo_k, hi_k = k << shift, min(n, (k + 1) << shift)
+                rays_d[lo_k:hi_k].copy_(host[lo_k:hi_k], non_blocking=True)
+                ready[k:k + 1].copy_(ones[k:k + 1], non_blocking=True)
+        assert _streamed(g, rays_d, out, ready, shift, any_hit, s) == abi.PBRT_OK
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.array_equal(got if any_hit else got.view(np.uint32), want), rep
+
+
+@pytest.mark.gpu
+def test_streamed_walk_gives_up_on_pieces_that_never_arrive():
+    """A piece whose flag nothing sets: the walk's bounded wait runs out,
+    the call returns PBRT_ERR_TIMEOUT, the pieces that did arrive are
+    traced, and the next call on the same handle works."""
+    torch = _torch()
+    import time
+    prims, _ = G.ray_soup(4096, 1, seed=7)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    n, shift = 1 << 17, 14
+    rays = G.incoherent_rays(G.PCG32(43), n, lo, hi)
+    want = dev_hits(g, rays).view(np.uint32).reshape(-1, 4)
+    rays_d = to_dev(rays)
+    ready = torch.zeros(n >> shift, dtype=torch.int32, device="cuda")
+    ready[:4] = 1  # pieces 0-3 arrived, 4-7 never do
+    out = torch.full((n, 4), 7.0, dtype=torch.float32, device="cuda")
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    assert _streamed(g, rays_d, out, ready, shift, False, s) == abi.PBRT_ERR_TIMEOUT
+    assert 1.5 < time.perf_counter() - t0 < 30.0
+    got = out.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got[:4 << shift], want[:4 << shift])
+    ready.fill_(1)
+    out.fill_(7.0)
+    torch.cuda.synchronize()
+    assert _streamed(g, rays_d, out, ready, shift, False, s) == abi.PBRT_OK
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
+    assert np.array_equal(dev_hits(g, rays).view(np.uint32).reshape(-1, 4), want)
