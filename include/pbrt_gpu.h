@@ -265,10 +265,12 @@ int pbrtgpu_bvh_get_primitive_order(const PbrtBVH* bvh, uint32_t* out,
  *  - streamed (default for rays in pinned memory, 2^17 rays or more, the
  *    default traversal kernel): the traversal on `stream` starts at once
  *    and the rays follow in pieces on the handle's copy stream, each warp
- *    waiting for the piece it takes (see pbrtgpu_intersect_streamed);
- *    closest hits go straight to device memory or to pinned host memory
- *    mapped into the device's address space, any-hit answers to host
- *    memory through one copy.  PBRT_STREAM_IN=0 turns it off;
+ *    waiting for the piece it takes (see pbrtgpu_intersect_streamed; a
+ *    walk whose pieces do not come within 50 ms + 2 ns per ray, e.g. under
+ *    a profiler that serialises work, is redone over the staged rays);
+ *    closest hits go straight to device memory or are written to pinned
+ *    host memory by the walk, any-hit answers to host memory through one
+ *    copy.  PBRT_STREAM_IN=0 turns it off;
  *  - in place (PBRT_HOST_MAPPED=1, pinned buffers): the traversal reads and
  *    writes the mapped host memory;
  *  - pipelined (every other host buffer): copies in and out and the

@@ -229,7 +229,12 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
             if (WIDE) {
                 Traversal4<S1, S2> T;
                 T.bind(smem_stack, threadIdx.x, blockDim.x);
-                const DevBVH4 bv = J.P.bvh4;
+                // by reference: the walk reads the tree's arrays from the job
+                // table (L1) instead of holding them in registers (80 -> 72,
+                // one more block per SM); the per-job mode keeps its copy
+                // (it spills without it)
+                const DevBVH4 bv_copy = MODE == kPerJob ? J.P.bvh4 : DevBVH4{};
+                const DevBVH4& bv = MODE == kPerJob ? bv_copy : J.P.bvh4;
                 if (T.start(bv, r)) {
                     if (any) {
                         while (T.template step<true>(bv, r)) {

@@ -183,14 +183,13 @@ static int scratch_pool(int dev, cudaMemPool_t* out) {
 // origin when the configuration asks for it (reorder.cu); the permutation
 // lives in stream-ordered scratch released on the same stream.
 static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* d_hits, uint8_t* d_occ,
-                        cudaStream_t s, const uint32_t* ready = nullptr, uint32_t piece_shift = 0,
-                        PbrtHit* host_hits = nullptr) {
+                        cudaStream_t s, StreamIn in = {}, PbrtHit* host_hits = nullptr) {
     const uint32_t* order = nullptr;
     uint32_t* work = nullptr;
     void* scratch = nullptr;
     int st;
-    const bool reorder = !ready && !host_hits && trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
-    const bool chunked = ready || host_hits || trace_chunk() != 0;
+    const bool reorder = !in.ready && !host_hits && trace_reorder() && n >= kReorderMinRays && !b->host.nodes.empty();
+    const bool chunked = in.ready || host_hits || trace_chunk() != 0;
     // [256 B: chunk counter, replay flag][permutation scratch]
     cudaMemPool_t pool = nullptr;
     if ((st = scratch_pool(b->device, &pool))) return st;
@@ -222,7 +221,7 @@ static int launch_batch(PbrtBVH* b, const PbrtRay* d_rays, uint32_t n, PbrtHit* 
         order = ord;
     }
     st = cuda_status(launch_trace(b->dev, b->host.depth, d_rays, n, d_hits, d_occ, b->d_status, s, wide_of(b),
-                                  b->host.stack4_bound, -1, order, work, replay, ready, piece_shift, host_hits),
+                                  b->host.stack4_bound, -1, order, work, replay, in, host_hits),
                      "trace launch");
     cudaFreeAsync(scratch, s);
     return st;
@@ -260,7 +259,7 @@ static void* mapped_host_pointer(const void* p) {
 // chunks (one compute stream: 1.82 / 1.87 / 2.04 ms).
 constexpr uint32_t kPipeChunkMin = 1u << 18;
 constexpr uint32_t kPipeChunks = 8;
-constexpr uint32_t kStreamPieces = 64;  // streamed input (trace_streamed): pieces per call at most
+constexpr uint32_t kStreamPieces = 16;  // streamed input (trace_streamed): pieces per call at most
 static uint32_t pipe_chunks() {
     static const uint32_t k = [] {
         const char* v = getenv("PBRT_PIPE_CHUNKS");
@@ -303,11 +302,12 @@ static int pipe_streams(PbrtBVH* b) {
 
 // Streamed host input.  Rays in pinned host memory, results in device
 // memory or (closest hits) in pinned host memory mapped into the device's
-// address space: the traversal is launched first, then the rays follow in
-// pieces of 2^shift rays (at most kStreamPieces, at least 2^kStreamShiftMin
-// rays each) on the copy stream, each piece's copy followed by a 4-byte copy
-// that sets the piece's flag.  The kernel's warps take rays in order and
-// wait (bounded) for the piece they need, so the traversal starts after the
+// address space: the rays go in pieces of 2^shift rays (at most
+// kStreamPieces, at least 2^kStreamShiftMin rays each) on the copy stream,
+// each piece's copy followed by a 4-byte copy that sets the piece's flag,
+// and the traversal is launched behind them on the caller's stream without
+// waiting for them.  The kernel's warps take rays in order and wait
+// (bounded) for the piece they need, so the traversal starts after the
 // first piece instead of after every copy, and one launch replaces the
 // copy pipeline's per-chunk launches.  Closest hits for host memory are
 // staged on the device and written out by the walk itself, each chunk of
@@ -352,11 +352,20 @@ static int trace_streamed(PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit* 
         (st = cuda_status(cudaEventRecord(b->pipe_ev[0], s), "cudaEventRecord")) ||
         (st = cuda_status(cudaStreamWaitEvent(b->pipe_in, b->pipe_ev[0], 0), "cudaStreamWaitEvent")))
         return st;
-    const int launch_st = launch_batch(b, d_rays, n, d_hits, d_occ, s, b->d_ready, shift, host_hits);
-    // the copies are queued whatever the launch did: a walk that did start
-    // waits for them
+    // A warp waits for a piece at most 50 ms + 2 ns per ray of the call
+    // (the copies move a ray in 0.15 ns); a walk that runs out (the copies
+    // did not run beside it) is redone below over the rays then staged.
+    const uint32_t wait_ms = 50u + (uint32_t)((2ull * n) / 1000000ull);
+    // The copies are queued before the launch (32 calls, a few microseconds
+    // of host time, while the first piece is already moving), so a walk that
+    // a profiler runs only after earlier work finds every piece landed.
+    // PBRT_TEST_HOLD_STREAM_COPIES=1 (tests) queues them only after the walk
+    // has given up instead, which exercises the redo.
+    const char* hold_env = getenv("PBRT_TEST_HOLD_STREAM_COPIES");
+    const bool hold = hold_env && hold_env[0] == '1';
+    const uint32_t pre = hold ? 0u : pieces;
     int copy_st = PBRT_OK;
-    for (uint32_t k = 0; k < pieces && !copy_st; ++k) {
+    auto enqueue = [&](uint32_t k) {
         const uint64_t lo = (uint64_t)k << shift;
         const uint64_t cnt = std::min<uint64_t>((uint64_t)n - lo, 1ull << shift);
         copy_st = cuda_status(cudaMemcpyAsync(d_rays + lo, rays + lo, cnt * sizeof(PbrtRay), cudaMemcpyHostToDevice,
@@ -366,9 +375,20 @@ static int trace_streamed(PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit* 
             copy_st = cuda_status(cudaMemcpyAsync(b->d_ready + k, b->h_one, sizeof(uint32_t), cudaMemcpyHostToDevice,
                                                   b->pipe_in),
                                   "cudaMemcpyAsync H2D");
-    }
-    if (!launch_st && !copy_st && occ && d_occ != occ)
-        copy_st = cuda_status(cudaMemcpyAsync(occ, d_occ, n, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
+    };
+    for (uint32_t k = 0; k < pre && !copy_st; ++k) enqueue(k);
+    const int launch_st =
+        copy_st ? PBRT_OK : launch_batch(b, d_rays, n, d_hits, d_occ, s, StreamIn{b->d_ready, shift, wait_ms}, host_hits);
+    if (hold) cudaStreamSynchronize(s);
+    // the held copies are queued whatever the launch did: a walk that did
+    // start waits for them
+    for (uint32_t k = pre; k < pieces && !copy_st; ++k) enqueue(k);
+    auto copy_back = [&]() {  // any-hit answers staged for host memory
+        return occ && d_occ != occ
+                   ? cuda_status(cudaMemcpyAsync(occ, d_occ, n, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H")
+                   : PBRT_OK;
+    };
+    if (!launch_st && !copy_st) copy_st = copy_back();
     // a walk whose pieces never come ends by itself (PBRT_ERR_TIMEOUT)
     const int sync_st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     const int sync_in = cuda_status(cudaStreamSynchronize(b->pipe_in), "cudaStreamSynchronize");
@@ -377,7 +397,24 @@ static int trace_streamed(PbrtBVH* b, const PbrtRay* rays, uint32_t n, PbrtHit* 
         device_status(b);  // clears a timeout the failed copies caused
         return first;
     }
-    return sync_st ? sync_st : sync_in;
+    if (sync_st || sync_in) return sync_st ? sync_st : sync_in;
+    int dev_status = 0;
+    if ((st = cuda_status(cudaMemcpy(&dev_status, b->d_status, sizeof(int), cudaMemcpyDeviceToHost), "status")))
+        return st;
+    if (dev_status == PBRT_ERR_TIMEOUT) {
+        // the walk gave up on pieces that had not landed; every copy has
+        // finished now, so the staged rays are traced again in full
+        cudaMemset(b->d_status, 0, sizeof(int));
+        if ((st = launch_batch(b, d_rays, n, d_hits, d_occ, s, StreamIn{}, host_hits)) || (st = copy_back()) ||
+            (st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize")))
+            return st;
+        return device_status(b);
+    }
+    if (dev_status) {
+        cudaMemset(b->d_status, 0, sizeof(int));
+        return set_error(dev_status, "device-side traversal failure");
+    }
+    return PBRT_OK;
 }
 
 // Runs closest/any hit for host or device buffers.
@@ -402,7 +439,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
         if (PbrtHit* mh = static_cast<PbrtHit*>(mapped_host_pointer(hits))) {
             std::lock_guard<std::mutex> lk(b->stage_mu);
             if ((st = b->stage_out.reserve((size_t)n * sizeof(PbrtHit))) ||
-                (st = launch_batch(b, rays, n, static_cast<PbrtHit*>(b->stage_out.p), nullptr, s, nullptr, 0, mh)) ||
+                (st = launch_batch(b, rays, n, static_cast<PbrtHit*>(b->stage_out.p), nullptr, s, StreamIn{}, mh)) ||
                 (st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize")))
                 return st;
             return device_status(b);
@@ -423,8 +460,7 @@ static int trace_call(const PbrtBVH* cb, const PbrtRay* rays, uint32_t n, PbrtHi
         trace_streams(b->dev, wide_of(b), b->host.stack4_bound, n)) {
         PbrtHit* d_hits = hits && !dout ? static_cast<PbrtHit*>(mapped_host_pointer(hits)) : hits;
         if (!hits || d_hits) {
-            if ((st = trace_streamed(b, rays, n, d_hits, occ, dout, s))) return st;
-            return device_status(b);
+            return trace_streamed(b, rays, n, d_hits, occ, dout, s);
         }
     }
     const PbrtRay* d_rays = rays;
@@ -708,7 +744,7 @@ int pbrtgpu_intersect_streamed(const PbrtBVH* cb, const PbrtRay* rays, uint32_t 
     if (!trace_streams(b->dev, wide_of(b), b->host.stack4_bound, n))
         return set_error(PBRT_ERR_UNSUPPORTED, "streamed rays need the 4-wide persistent walk with a work counter");
     cudaStream_t s = (cudaStream_t)stream;
-    if ((st = launch_batch(b, rays, n, hits, occluded, s, ready, piece_shift))) return st;
+    if ((st = launch_batch(b, rays, n, hits, occluded, s, StreamIn{ready, piece_shift, 2000}))) return st;
     if ((st = cuda_status(cudaStreamSynchronize(s), "cudaStreamSynchronize"))) return st;
     return device_status(b);
 }

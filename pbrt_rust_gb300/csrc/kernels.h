@@ -59,18 +59,25 @@ int trace_stack_for_depth(uint32_t depth);
 // hit: required; a device word, zero at launch) flags that some ray's walk
 // accepted a NaN distance; a replay kernel queued after the traversal then
 // rewrites those rays' hits by the exact walk (see Traversal in trace.cuh).
-// `ready` (streamed input; needs `work` and trace_streams()): the rays arrive
-// in pieces of 2^piece_shift rays while the walk runs, ready[k] (zero at
-// launch) turning non-zero once piece k has landed; a piece that has not
-// landed within 2 s ends the walk with PBRT_ERR_TIMEOUT in d_status.
+// `in.ready` (streamed input; needs `work` and trace_streams()): the rays
+// arrive in pieces of 2^in.shift rays while the walk runs, in.ready[k] (zero
+// at launch) turning non-zero once piece k has landed; a piece that has not
+// landed within in.wait_ms ends the walk with PBRT_ERR_TIMEOUT in d_status.
 // `host_hits` (closest hits; needs `work` and trace_streams()): pinned host
 // memory mapped into the device's address space that receives the hits,
 // chunk by chunk as they complete; `hits` is then the device staging array.
+// Streamed input of a walk: piece flags (null: the rays are all there),
+// rays per piece (2^shift) and how long a warp waits for a piece.
+struct StreamIn {
+    const uint32_t* ready = nullptr;
+    uint32_t shift = 0;
+    uint32_t wait_ms = 0;
+};
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide = nullptr,
                          uint32_t wide_bound = 0, int kernel = -1, const uint32_t* order = nullptr,
-                         uint32_t* work = nullptr, uint32_t* replay = nullptr, const uint32_t* ready = nullptr,
-                         uint32_t piece_shift = 0, PbrtHit* host_hits = nullptr);
+                         uint32_t* work = nullptr, uint32_t* replay = nullptr, StreamIn in = {},
+                         PbrtHit* host_hits = nullptr);
 // Whether the configured traversal of this tree can take streamed input
 // (the 4-wide persistent walk with its shared counter, rays in order).
 bool trace_streams(const DevBVH& bvh, const DevBVH4* wide, uint32_t wide_bound, uint32_t n);

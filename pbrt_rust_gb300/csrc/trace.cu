@@ -177,17 +177,16 @@ __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-// A piece's copy takes well under a millisecond; two seconds without its
-// flag means the copies never ran, and the warp gives up instead of hanging
-// (at once when another warp already gave up: *status holds the timeout).
-constexpr uint64_t kPieceWaitNs = 2000000000ull;
-__device__ __noinline__ bool wait_piece(const uint32_t* ready, uint32_t k, const int* status) {
+// A flag that has not come within `wait_ms` means the copies did not run
+// beside the walk (or at all), and the warp gives up instead of hanging (at
+// once when another warp already gave up: *status holds the timeout).
+__device__ __noinline__ bool wait_piece(const uint32_t* ready, uint32_t k, uint32_t wait_ms, const int* status) {
     if (ld_acquire_u32(ready + k)) return true;
-    const uint64_t t0 = global_ns();
+    const uint64_t t0 = global_ns(), limit = (uint64_t)wait_ms * 1000000ull;
     for (;;) {
         __nanosleep(256);
         if (ld_acquire_u32(ready + k)) return true;
-        if (global_ns() - t0 > kPieceWaitNs ||
+        if (global_ns() - t0 > limit ||
             ld_acquire_u32(reinterpret_cast<const uint32_t*>(status)) == (uint32_t)PBRT_ERR_TIMEOUT)
             return false;
     }
@@ -238,8 +237,7 @@ __global__ void __launch_bounds__(128, MINB)
                         const uint32_t* __restrict__ order,
                         float4* __restrict__ hits, uint8_t* __restrict__ occ, int* __restrict__ status,
                         uint32_t per_warp, uint32_t refill, uint32_t* __restrict__ work,
-                        uint32_t* __restrict__ replay, const uint32_t* __restrict__ ready, uint32_t piece_shift,
-                        float4* __restrict__ host_hits) {
+                        uint32_t* __restrict__ replay, const StreamIn in, float4* __restrict__ host_hits) {
     static_assert(!(HOSTOUT && ANY), "host write-out is for closest hits");
     extern __shared__ uint2 smem_stack[];
     const unsigned lane = threadIdx.x & 31u;
@@ -307,10 +305,10 @@ __global__ void __launch_bounds__(128, MINB)
                 if (base < n) {
                     next = base;
                     end = (Pos)((uint64_t)base + per_warp < (uint64_t)n ? (uint64_t)base + per_warp : (uint64_t)n);
-                    if (ready) {  // streamed input: the chunk's rays must have landed
+                    if (in.ready) {  // streamed input: the chunk's rays must have landed
                         int ok = 1;
                         if (lane == 0)
-                            ok = wait_piece(ready, (uint32_t)((end - 1) >> piece_shift), status) ? 1 : 0;
+                            ok = wait_piece(in.ready, (uint32_t)((end - 1) >> in.shift), in.wait_ms, status) ? 1 : 0;
                         if (!__shfl_sync(0xffffffffu, ok, 0)) {
                             if (lane == 0) atomicMax(status, PBRT_ERR_TIMEOUT);
                             next = end;
@@ -344,7 +342,7 @@ __global__ void __launch_bounds__(128, MINB)
                         ring[10 + lane] = ring[8];
                     }
                     const float4* rp = rays + 2 * (size_t)ray;
-                    r = ready ? make_dray(__ldcg(rp), __ldcg(rp + 1)) : make_dray(__ldg(rp), __ldg(rp + 1));
+                    r = in.ready ? make_dray(__ldcg(rp), __ldcg(rp + 1)) : make_dray(__ldg(rp), __ldg(rp + 1));
                     bool live = T.start(bvh, r);
                     if (!live) {
                         if (ANY)
@@ -577,8 +575,8 @@ __global__ void __launch_bounds__(128) k_replay2(const __grid_constant__ DevBVH 
 template <int SMAX, int OVF, bool ANY, int MINB, bool INST = false, bool HOSTOUT = false>
 static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, uint32_t n, const uint32_t* order,
                                           float4* h4, uint8_t* occ, int* d_status, cudaStream_t stream,
-                                          uint32_t* work, uint32_t* replay, const uint32_t* ready = nullptr,
-                                          uint32_t piece_shift = 0, float4* host_hits = nullptr) {
+                                          uint32_t* work, uint32_t* replay, StreamIn in = {},
+                                          float4* host_hits = nullptr) {
     const int block = 128;
     // HOSTOUT: each warp's ring after the stacks
     const size_t smem = (size_t)SMAX * sizeof(uint2) * block + (HOSTOUT ? (block / 32) * kRingWords * sizeof(uint32_t) : 0);
@@ -595,16 +593,16 @@ static cudaError_t launch_wide_persistent(const DevBVH4& bvh, const float4* r4, 
         uint64_t w = chunks < warps ? chunks : warps;
         unsigned grid = (unsigned)((w + (block / 32) - 1) / (block / 32));
         k_trace4_persistent<SMAX, OVF, ANY, MINB, INST, HOSTOUT><<<grid, block, smem, stream>>>(
-            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work, replay, ready, piece_shift, host_hits);
+            bvh, r4, n, order, h4, occ, d_status, g_chunk, g_refill, work, replay, in, host_hits);
         return cudaGetLastError();
     }
     // fixed per-warp ranges would read rays out of order and have no chunks
     // to write out: no streamed input, no write-out
-    if (ready || HOSTOUT) return cudaErrorInvalidValue;
+    if (in.ready || HOSTOUT) return cudaErrorInvalidValue;
     uint64_t need_warps = (n + per_warp - 1) / per_warp;
     unsigned grid = (unsigned)((need_warps + (block / 32) - 1) / (block / 32));
     k_trace4_persistent<SMAX, OVF, ANY, MINB, INST, HOSTOUT><<<grid, block, smem, stream>>>(
-        bvh, r4, n, order, h4, occ, d_status, per_warp, g_refill, nullptr, replay, nullptr, 0, nullptr);
+        bvh, r4, n, order, h4, occ, d_status, per_warp, g_refill, nullptr, replay, StreamIn{}, nullptr);
     return cudaGetLastError();
 }
 
@@ -842,8 +840,8 @@ bool trace_streams(const DevBVH& bvh, const DevBVH4* wide, uint32_t wide_bound, 
 // walk with its shared counter (the only kernel that takes rays in order).
 static cudaError_t launch_streamed(const DevBVH& bvh, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                                    uint8_t* occ, int* d_status, cudaStream_t stream, const DevBVH4* wide,
-                                   uint32_t wide_bound, uint32_t* work, uint32_t* replay, const uint32_t* ready,
-                                   uint32_t shift, PbrtHit* host_hits) {
+                                   uint32_t wide_bound, uint32_t* work, uint32_t* replay, StreamIn in,
+                                   PbrtHit* host_hits) {
     if (!work || !trace_streams(bvh, wide, wide_bound, n) || (host_hits && occ)) return cudaErrorInvalidValue;
     const float4* r4 = reinterpret_cast<const float4*>(rays);
     float4* h4 = reinterpret_cast<float4*>(hits);
@@ -852,51 +850,51 @@ static cudaError_t launch_streamed(const DevBVH& bvh, const PbrtRay* rays, uint3
         float4* hh = reinterpret_cast<float4*>(host_hits);
         if (wide_stack_variant(wide_bound) == 64)
             return inst ? launch_wide_persistent<16, 48, false, 0, true, true>(*wide, r4, n, nullptr, h4, nullptr,
-                                                                              d_status, stream, work, replay, ready,
-                                                                              shift, hh)
+                                                                              d_status, stream, work, replay, in,
+                                                                              hh)
                         : launch_wide_persistent<16, 48, false, 0, false, true>(*wide, r4, n, nullptr, h4, nullptr,
-                                                                               d_status, stream, work, replay, ready,
-                                                                               shift, hh);
+                                                                               d_status, stream, work, replay, in,
+                                                                               hh);
         return inst ? launch_wide_persistent<16, 240, false, 0, true, true>(*wide, r4, n, nullptr, h4, nullptr,
-                                                                           d_status, stream, work, replay, ready,
-                                                                           shift, hh)
+                                                                           d_status, stream, work, replay, in,
+                                                                           hh)
                     : launch_wide_persistent<16, 240, false, 0, false, true>(*wide, r4, n, nullptr, h4, nullptr,
-                                                                            d_status, stream, work, replay, ready,
-                                                                            shift, hh);
+                                                                            d_status, stream, work, replay, in,
+                                                                            hh);
     }
     if (wide_stack_variant(wide_bound) == 64) {
         if (inst)
             return any ? launch_wide_persistent<16, 48, true, 0, true>(*wide, r4, n, nullptr, nullptr, occ, d_status,
-                                                                       stream, work, replay, ready, shift)
+                                                                       stream, work, replay, in)
                        : launch_wide_persistent<16, 48, false, 0, true>(*wide, r4, n, nullptr, h4, nullptr, d_status,
-                                                                        stream, work, replay, ready, shift);
+                                                                        stream, work, replay, in);
         return any ? launch_wide_persistent<16, 48, true, 0>(*wide, r4, n, nullptr, nullptr, occ, d_status, stream,
-                                                             work, replay, ready, shift)
+                                                             work, replay, in)
                    : launch_wide_persistent<16, 48, false, 0>(*wide, r4, n, nullptr, h4, nullptr, d_status, stream,
-                                                              work, replay, ready, shift);
+                                                              work, replay, in);
     }
     if (inst)
         return any ? launch_wide_persistent<16, 240, true, 0, true>(*wide, r4, n, nullptr, nullptr, occ, d_status,
-                                                                    stream, work, replay, ready, shift)
+                                                                    stream, work, replay, in)
                    : launch_wide_persistent<16, 240, false, 0, true>(*wide, r4, n, nullptr, h4, nullptr, d_status,
-                                                                     stream, work, replay, ready, shift);
+                                                                     stream, work, replay, in);
     return any ? launch_wide_persistent<16, 240, true, 0>(*wide, r4, n, nullptr, nullptr, occ, d_status, stream,
-                                                          work, replay, ready, shift)
+                                                          work, replay, in)
                : launch_wide_persistent<16, 240, false, 0>(*wide, r4, n, nullptr, h4, nullptr, d_status, stream, work,
-                                                           replay, ready, shift);
+                                                           replay, in);
 }
 
 cudaError_t launch_trace(const DevBVH& bvh, uint32_t depth, const PbrtRay* rays, uint32_t n, PbrtHit* hits,
                          uint8_t* occluded, int* d_status, cudaStream_t stream, const DevBVH4* wide,
                          uint32_t wide_bound, int kernel, const uint32_t* order, uint32_t* work, uint32_t* replay,
-                         const uint32_t* ready, uint32_t piece_shift, PbrtHit* host_hits) {
+                         StreamIn in, PbrtHit* host_hits) {
     if (n == 0) return cudaSuccess;
     if (!occluded && !replay) return cudaErrorInvalidValue;
     read_variant();
-    if ((ready || host_hits) && order) return cudaErrorInvalidValue;
-    cudaError_t e = ready || host_hits
+    if ((in.ready || host_hits) && order) return cudaErrorInvalidValue;
+    cudaError_t e = in.ready || host_hits
                         ? launch_streamed(bvh, rays, n, hits, occluded, d_status, stream, wide, wide_bound, work,
-                                          replay, ready, piece_shift, host_hits)
+                                          replay, in, host_hits)
                         : launch_main(bvh, depth, rays, n, hits, occluded, d_status, stream, wide, wide_bound, kernel,
                                       order, work, replay);
     if (e != cudaSuccess || occluded) return e;

@@ -1,12 +1,14 @@
 """Standalone workloads for profilers (ncu) and quick timing.
 
-  python -m pbrt_rust_gb300.profile trace  [--rays N] [--any] [--repeat R]
+  python -m pbrt_rust_gb300.profile trace  [--rays N] [--any] [--host-out] [--repeat R]
   python -m pbrt_rust_gb300.profile render [--res R] [--spp-side S] [--repeat R]
   python -m pbrt_rust_gb300.profile batch  [--scenes N] [--repeat R]
   python -m pbrt_rust_gb300.profile served [--scenes N] [--requests Q] [--slots K] [--repeat R]
 
 `trace` and `render` use the 708x708 heightfield scene; `trace` runs R
-closest-hit (or any-hit) passes over N incoherent rays, `render` R frames of
+closest-hit (or any-hit) passes over N incoherent rays (with --host-out the
+closest hits go to pinned host memory: the walk that writes them out chunk
+by chunk), `render` R frames of
 the direct-lighting wavefront.  `batch` renders the multi-scene workload
 (N scenes of 1k-256k triangles + 0-32 spheres, 128-512 squared, 1/4/16 spp)
 as one batch R times, with the tuning the autotuner picks for it (binary
@@ -107,6 +109,7 @@ def main(argv=None) -> int:
     ap.add_argument("--scenes", type=int, default=64)
     ap.add_argument("--rays", type=int, default=1 << 20)
     ap.add_argument("--any", action="store_true")
+    ap.add_argument("--host-out", action="store_true", help="trace: closest hits into pinned host memory")
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--res", type=int, default=256)
     ap.add_argument("--spp-side", type=int, default=2)
@@ -180,7 +183,9 @@ def main(argv=None) -> int:
         bvh = GpuBVHAccel(prims, 4, "sah")
         rd = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
         out = torch.empty((a.rays, 4) if not a.any else (a.rays,), dtype=torch.float32 if not a.any else torch.uint8,
-                          device="cuda")
+                          device="cpu" if a.host_out and not a.any else "cuda")
+        if a.host_out and not a.any:
+            out = out.pin_memory()
         fn = lib.pbrtgpu_intersect_p if a.any else lib.pbrtgpu_intersect
         for _ in range(a.repeat):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

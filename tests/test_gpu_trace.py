@@ -463,6 +463,35 @@ def test_pinned_host_buffers_every_form(monkeypatch, form):
     assert np.array_equal(pocc.numpy(), want_any)
 
 
+@pytest.mark.gpu
+def test_streamed_form_recovers_when_the_copies_come_late(monkeypatch):
+    """When the ray copies do not run beside the streamed walk (as under a
+    profiler that serialises work; PBRT_TEST_HOLD_STREAM_COPIES=1 queues them
+    only after the walk has given up), the walk's bounded wait runs out and
+    the call traces the staged rays again: same results, bounded delay."""
+    import time
+    torch = _torch()
+    prims, _ = G.ray_soup(4096, 1, seed=8)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    rays = G.incoherent_rays(G.PCG32(47), (1 << 18) + 55, lo, hi)
+    want, want_any = dev_hits(g, rays), dev_any(g, rays)
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    monkeypatch.setenv("PBRT_TEST_HOLD_STREAM_COPIES", "1")
+    out = torch.full((len(rays), 4), 7.0, dtype=torch.float32).pin_memory()
+    t0 = time.perf_counter()
+    g.intersect(pinned, out=out)
+    assert 0.04 < time.perf_counter() - t0 < 5.0
+    assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    occ = torch.full((len(rays),), 9, dtype=torch.uint8).pin_memory()
+    g.intersect_p(pinned, out=occ)
+    assert np.array_equal(occ.numpy(), want_any)
+    monkeypatch.delenv("PBRT_TEST_HOLD_STREAM_COPIES")
+    out.fill_(7.0)
+    g.intersect(pinned, out=out)  # and the next call streams normally
+    assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+
+
 def _streamed(bvh, rays_d, out_d, ready, shift, any_hit, stream):
     import ctypes as C
     lib = abi.load()
