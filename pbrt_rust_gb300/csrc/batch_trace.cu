@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
                 res = T.res;
                 fail = T.overflow ? 6 : 0;
             } else {
-                const DevBVH bv = J.P.bvh;
+                const DevBVH& bv = J.P.bvh;  // from the job table, as above
                 found = any ? traverse<S1, true, S2 != 0>(bv, r, &res, &fail)
                             : traverse<S1, false, S2 != 0>(bv, r, &res, &fail, &nan);
             }
