@@ -400,6 +400,38 @@ def test_nonfinite_vertices_match_oracle(oracle, name):
         abi.set_trace_config(**before)
 
 
+def test_nonfinite_vertices_from_pinned_host_memory(oracle):
+    """The NaN-distance case through the host-buffer forms: rays in pinned
+    memory (16 copies of the degenerate set, enough for the streamed form),
+    closest hits written out to pinned memory by the walk and the marked
+    ones rewritten there by the exact replay; pipelined and in place too.
+    Equal to the oracle (NaN payloads aside)."""
+    import os
+    torch = _torch()
+    mesh, rays = degenerate_scene_and_rays(nonfinite=True)
+    rays = np.tile(rays, 16)
+    g, o = GpuBVHAccel([mesh], 1, "sah"), oracle.OracleBVH([mesh], 1, "sah")
+    want, want_any = o.intersect(rays), o.intersect_p(rays)
+    assert np.isnan(want["t"]).sum() > 800
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    saved = {k: os.environ.get(k) for k in ("PBRT_STREAM_IN", "PBRT_HOST_MAPPED")}
+    try:
+        for stream_in, mapped in (("1", "0"), ("0", "0"), ("1", "1")):
+            os.environ["PBRT_STREAM_IN"], os.environ["PBRT_HOST_MAPPED"] = stream_in, mapped
+            out = torch.full((len(rays), 4), 7.0, dtype=torch.float32).pin_memory()
+            g.intersect(pinned, out=out)
+            assert same_hits(out.numpy().view(abi.HIT_DTYPE).reshape(-1), want), (stream_in, mapped)
+            occ = torch.full((len(rays),), 9, dtype=torch.uint8).pin_memory()
+            g.intersect_p(pinned, out=occ)
+            assert np.array_equal(occ.numpy(), want_any), (stream_in, mapped)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def test_pipelined_host_buffers_equal_device_buffers():
     """Host-buffer calls of 2^19+ rays run in chunks whose copies overlap
     the other chunks' traversal; every hit must land as with device
@@ -490,6 +522,70 @@ def test_streamed_form_recovers_when_the_copies_come_late(monkeypatch):
     out.fill_(7.0)
     g.intersect(pinned, out=out)  # and the next call streams normally
     assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [(1 << 17) - 1, 1 << 17, (1 << 17) + 1, 3 * (1 << 16) + 5, (1 << 21) + 3])
+def test_streamed_form_at_its_piece_boundaries(n):
+    """Ray counts either side of the streamed form's threshold (2^17) and of
+    its piece sizes (2^16 rays, more for 2^21 + 3 rays: 16 pieces of 2^17):
+    pinned host rays and hits equal the device-buffer results."""
+    torch = _torch()
+    prims, _ = G.ray_soup(2048, 1, seed=9)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    rays = G.incoherent_rays(G.PCG32(53), n, lo, hi)
+    want, want_any = dev_hits(g, rays), dev_any(g, rays)
+    pinned = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    out = torch.full((n, 4), 7.0, dtype=torch.float32).pin_memory()
+    g.intersect(pinned, out=out)
+    assert np.array_equal(out.numpy().view(np.uint32).reshape(-1), want.view(np.uint32).reshape(-1))
+    occ = torch.full((n,), 9, dtype=torch.uint8).pin_memory()
+    g.intersect_p(pinned, out=occ)
+    assert np.array_equal(occ.numpy(), want_any)
+
+
+@pytest.mark.gpu
+def test_host_buffer_calls_from_several_threads():
+    """Four host threads share one handle, each with its own stream and its
+    own pinned or pageable buffers: the calls serialise on the handle's
+    staging buffers and flags, and every result equals the device-buffer
+    one."""
+    import threading
+    torch = _torch()
+    prims, _ = G.ray_soup(4096, 1, seed=10)
+    g = GpuBVHAccel(prims, 4, "sah")
+    lo, hi = np.array([-1.5] * 3, np.float32), np.array([1.5] * 3, np.float32)
+    sets = [G.incoherent_rays(G.PCG32(60 + k), (1 << 18) + 17 * k, lo, hi) for k in range(4)]
+    wants = [(dev_hits(g, r).view(np.uint32).reshape(-1), dev_any(g, r)) for r in sets]
+    errors = []
+
+    def work(k):
+        try:
+            stream = torch.cuda.Stream()
+            host = torch.from_numpy(sets[k].view(np.float32).reshape(-1, 8).copy())
+            if k % 2 == 0:
+                host = host.pin_memory()
+            for _ in range(3):
+                out = torch.full((len(sets[k]), 4), 7.0, dtype=torch.float32)
+                occ = torch.full((len(sets[k]),), 9, dtype=torch.uint8)
+                if k % 2 == 0:
+                    out, occ = out.pin_memory(), occ.pin_memory()
+                g.intersect(host, out=out, stream=stream)
+                g.intersect_p(host, out=occ, stream=stream)
+                if not np.array_equal(out.numpy().view(np.uint32).reshape(-1), wants[k][0]):
+                    errors.append(f"thread {k}: closest hits differ")
+                if not np.array_equal(occ.numpy(), wants[k][1]):
+                    errors.append(f"thread {k}: any hits differ")
+        except Exception as e:  # reported below
+            errors.append(f"thread {k}: {e!r}")
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
 
 
 def _streamed(bvh, rays_d, out_d, ready, shift, any_hit, stream):
