@@ -260,16 +260,19 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000,
     # the plain path with each render kernel (identical outputs): the
     # library's default and the 4-wide walk, which these scenes favour
     before = abi.get_trace_config()
-    plain_s = {}
+    plain_s, plain_lat = {}, {}
     for rk in ("plain", "w4"):
         abi.set_trace_config(render_kernel=rk)
         run_plain(reqs[:20], stream)
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        run_plain(reqs, stream)
+        plain_lat[rk] = run_plain(reqs, stream)
         plain_s[rk] = time.perf_counter() - t0
     abi.set_trace_config(**before)
     default_rk = before["render_kernel"] if before["render_kernel"] in plain_s else "plain"
+
+    def pct(lat, q):  # milliseconds
+        return float(np.percentile(np.asarray(lat) * 1e3, q))
     ref = [r[3].clone() for r in reqs]
     srv = GpuServer(slots=slots, pool_bytes=POOL_BYTES, max_jobs=256, max_samples=1 << 24, max_film_pixels=1 << 22,
                     max_query_rays=1 << 20, max_tasks=1 << 14)
@@ -284,11 +287,16 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000,
         raise RuntimeError("served results differ from the one-request results")
     sweep = []
     for k, rate in enumerate(rates):
-        st = run_served(srv, reqs, outs, G.poisson_arrivals(len(reqs), rate, seed=9 + k))
+        arrivals = G.poisson_arrivals(len(reqs), rate, seed=9 + k)
+        st = run_served(srv, reqs, outs, arrivals)
+        # the plain path under the same arrivals: one request at a time, a
+        # request waiting while the one before it runs
+        lat = run_plain(reqs, stream, arrivals)
         sweep.append({"rate": rate, "requests": st["completed"], "requests_per_s": st["requests_per_s"],
                       "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
                       "max_ms": st["max_ms"], "mean_batch": st["mean_batch_requests"], "deferred": st["deferred"],
-                      "refused": st["refused"]})
+                      "refused": st["refused"], "plain_p50_ms": pct(lat, 50), "plain_p99_ms": pct(lat, 99),
+                      "plain_mean_ms": float(np.mean(lat) * 1e3)})
     final = srv.stats()
     srv.close()
     n_render = sum(1 for r in reqs if r[0] == "render")
@@ -299,6 +307,9 @@ def bench_served(torch, dev, stream, n_scenes: int = 32, n_requests: int = 2000,
             "speedup": flood["requests_per_s"] * plain_s[default_rk] / len(reqs),
             "speedup_vs_fastest_plain": flood["requests_per_s"] * min(plain_s.values()) / len(reqs),
             "flood_p50_ms": flood["p50_ms"], "flood_p99_ms": flood["p99_ms"],
+            "plain_latency_ms": {"p50": pct(plain_lat[default_rk], 50), "p99": pct(plain_lat[default_rk], 99),
+                                 "mean": float(np.mean(plain_lat[default_rk]) * 1e3),
+                                 "how": "each request alone through its one-request call, back to back"},
             "flood_mean_batch": flood["mean_batch_requests"], "flood_deferred": flood["deferred"],
             "pool": {"budget_bytes": POOL_BYTES, "slot_bytes": final["slot_bytes"],
                      "resident_bytes": final["resident_bytes"], "resident_scenes": final["resident_count"],

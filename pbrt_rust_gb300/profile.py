@@ -75,15 +75,28 @@ def serving_requests(pool, n_requests: int, device, seed: int | None = None):
     return reqs
 
 
-def run_plain(reqs, stream) -> None:
+def run_plain(reqs, stream, arrivals=None) -> list:
     """Every request through its one-request call, each finished before the
-    next starts (renders return after the frame; queries synchronise)."""
-    for r in reqs:
+    next starts (renders return after the frame; queries synchronise); with
+    `arrivals` (seconds from the start) a request starts no earlier than its
+    arrival.  Returns each request's latency in seconds: completion minus
+    arrival (minus its own start without arrivals)."""
+    lat = []
+    t0 = time.perf_counter()
+    for k, r in enumerate(reqs):
+        if arrivals is not None:
+            while time.perf_counter() - t0 < arrivals[k]:
+                pass
+            start = t0 + arrivals[k]
+        else:
+            start = time.perf_counter()
         if r[0] == "render":
             r[2].render(r[1], out=r[3], stream=stream)
         else:
             r[1].intersect(r[2], out=r[3], stream=stream)
             stream.synchronize()
+        lat.append(time.perf_counter() - start)
+    return lat
 
 
 def run_served(srv, reqs, outs, arrivals=None) -> dict:
