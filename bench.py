@@ -80,14 +80,38 @@ def measured_peak():
 
 
 def committed_traffic():
-    """dram__bytes_read.sum + dram__bytes_write.sum of one closest-hit launch
-    on this workload, from the committed ncu summary (None without one)."""
+    """dram__bytes_read.sum + dram__bytes_write.sum, warp instructions and
+    lanes active per instruction of one closest-hit launch on this workload,
+    from the committed ncu summary (None without one)."""
     p = ROOT / "profiles" / "k_trace4_persistent_heightfield_4M_rays.md"
     if p.exists():
-        m = re.search(r"^dram_bytes_per_launch = (\d+)$", p.read_text(), re.M)
+        text = p.read_text()
+        m = re.search(r"^dram_bytes_per_launch = (\d+)$", text, re.M)
         if m:
-            return {"dram_bytes_per_launch": int(m.group(1)), "source": str(p.relative_to(ROOT))}
+            out = {"dram_bytes_per_launch": int(m.group(1)), "source": str(p.relative_to(ROOT))}
+            w = re.search(r"^warp_instructions_per_launch = (\d+)$", text, re.M)
+            a = re.search(r"^lanes_active_per_instruction = ([0-9.]+)$", text, re.M)
+            if w and a:
+                out["warp_instructions_per_launch"] = int(w.group(1))
+                out["lanes_active_per_instruction"] = float(a.group(1))
+            return out
     return None
+
+
+def issue_view(torch, tr, mean_ms, clocks):
+    """What bounds the headline kernel: its warp instructions per launch
+    (committed ncu summary) over this run's launch time, against the issue
+    peak of the device at the median SM clock of this run (one instruction
+    per scheduler per cycle, 4 schedulers per SM), and the lanes active per
+    instruction."""
+    if not tr or "warp_instructions_per_launch" not in tr or not clocks.get("sm_mhz"):
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    rate = tr["warp_instructions_per_launch"] / (mean_ms / 1e3)
+    peak = sms * 4 * clocks["sm_mhz"] * 1e6
+    lanes = tr["lanes_active_per_instruction"]
+    return {"warp_instructions_per_s": rate, "peak": peak, "frac": rate / peak, "lanes_active": lanes,
+            "thread_frac": rate / peak * lanes / 32.0, "source": tr["source"]}
 
 
 class ClockSampler:
@@ -788,7 +812,8 @@ def run_ours(args):
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": (tr or {}).get("dram_bytes_per_launch"),
                          "algorithmic_bytes_per_ray": bpr, "nodes_tested_per_ray": nodes_pr,
-                         "tris_tested_per_ray": tris_pr},
+                         "tris_tested_per_ray": tris_pr,
+                         "issue": issue_view(torch, tr, mean_ms, clk.summary())},
             "cpu_baseline": {"value": cpu_rps / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
                              "sample": f"{cpu_passes} passes over the 2^22 rays, {cpu_dt:.1f} s"},
             "e2e": {"value": e2e_mrays, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
