@@ -163,6 +163,15 @@ __global__ void __launch_bounds__(128) k_trace4(const __grid_constant__ DevBVH4 
     }
 }
 
+// A ray is read once: its lines go to L2 only, leaving L1 to the tree.
+__device__ __forceinline__ float4 ld_stream(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p));
+    return v;
+}
+
 // Streamed input: the rays arrive in pieces of 2^piece_shift rays while the
 // traversal already runs, and ready[k] turns non-zero once piece k has
 // landed (the copy stream writes it with a 4-byte copy queued behind the
@@ -268,7 +277,12 @@ __global__ void __launch_bounds__(128, MINB)
         __syncwarp();
     }
     auto put = [&](float4 h) {
-        hits[ray] = h;
+        // written once and not read here: streaming, except the staged hits
+        // that the write-out reads back
+        if constexpr (HOSTOUT)
+            hits[ray] = h;
+        else
+            __stcs(hits + ray, h);
         if constexpr (HOSTOUT) {
             uint32_t* ring = ring_of();
             const uint32_t j = ring[10 + lane];
@@ -342,7 +356,7 @@ __global__ void __launch_bounds__(128, MINB)
                         ring[10 + lane] = ring[8];
                     }
                     const float4* rp = rays + 2 * (size_t)ray;
-                    r = in.ready ? make_dray(__ldcg(rp), __ldcg(rp + 1)) : make_dray(__ldg(rp), __ldg(rp + 1));
+                    r = in.ready ? make_dray(__ldcg(rp), __ldcg(rp + 1)) : make_dray(ld_stream(rp), ld_stream(rp + 1));
                     bool live = T.start(bvh, r);
                     if (!live) {
                         if (ANY)
