@@ -291,10 +291,10 @@ int pbrtgpu_intersect_p(const PbrtBVH* bvh, const PbrtRay* rays, uint32_t n,
 /* Closest hits (hits non-NULL) or any-hit answers (occluded non-NULL),
  * device buffers only, for rays that arrive while the walk runs: piece k,
  * rays [k << piece_shift, (k + 1) << piece_shift), may be read once
- * ready[k] != 0 (ready: device memory, one uint32 per piece).  Set the
- * flags with copies (cudaMemcpyAsync on another stream) or host writes to
- * mapped memory, never from a kernel: the walk may hold every SM until the
- * flags are set.  piece_shift in [5, 31].  Needs the 4-wide persistent walk
+ * ready[k] != 0 (ready: device memory, one uint32 per piece).  Set each
+ * flag with a copy queued behind its piece's copy on another stream
+ * (cudaMemcpyAsync of a non-zero word), never from a kernel: the walk may
+ * hold every SM until the flags are set.  piece_shift in [5, 31].  Needs the 4-wide persistent walk
  * with its work counter (the default configuration; PBRT_ERR_UNSUPPORTED
  * otherwise).  Returns after the walk; a piece whose flag is not set within
  * 2 s ends the call with PBRT_ERR_TIMEOUT and its rays get no result.  The
