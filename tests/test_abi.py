@@ -57,6 +57,25 @@ def test_invalid_arguments_fail_loudly(lib):
         Shape.triangle_mesh(Transform(), None, False, [0, 1], np.zeros((3, 3)))
 
 
+def test_streamed_walk_arguments_are_checked(lib):
+    """pbrtgpu_intersect_streamed refuses a NULL handle, NULL rays or flags,
+    both or neither output and a piece size outside 2^5..2^31 before it
+    touches a device; a GPU-less host gets a status, never a CPU walk."""
+    f = lib.pbrtgpu_intersect_streamed
+    P = C.c_void_p
+    buf = (C.c_uint32 * 64)()
+    ptr = P(C.addressof(buf))
+    assert f(None, ptr, 4, ptr, None, ptr, 16, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    fake = P(1)  # never dereferenced: every check below fails first
+    assert f(fake, None, 4, ptr, None, ptr, 16, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    assert f(fake, ptr, 4, ptr, None, None, 16, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    assert f(fake, ptr, 4, ptr, ptr, ptr, 16, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    assert f(fake, ptr, 4, None, None, ptr, 16, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    for shift in (0, 4, 32, 40):
+        assert f(fake, ptr, 4, ptr, None, ptr, shift, None) == abi.PBRT_ERR_INVALID_ARGUMENT
+    assert f(fake, ptr, 0, ptr, None, ptr, 16, None) == abi.PBRT_OK  # nothing to do
+
+
 def test_bad_mesh_index_is_rejected(lib):
     d = abi.PbrtShapeDesc()
     pts = np.zeros(9, np.float32)
