@@ -432,8 +432,8 @@ typedef struct PbrtBatchLimits {
 
 /* Launch choices of a batch (the autotuner's search space).  A new batch
  * starts with 4-wide extend and shadow walks (binary where a job's tree has
- * no 4-wide layout), 128 threads, 16 stack entries, chunk 64, refill 32 /
- * 32, graphs on. */
+ * no 4-wide layout), 128 threads, 16 stack entries, chunk 64, refill 32
+ * (extend) / 8 (shadow), graphs on. */
 typedef struct PbrtBatchTuning {
     int32_t extend_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: camera and query rays */
     int32_t shadow_kernel;  /* PBRT_TRACE_PAIR or PBRT_TRACE_WIDE: shadow rays */

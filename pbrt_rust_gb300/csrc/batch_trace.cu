@@ -268,6 +268,100 @@ __global__ void __launch_bounds__(BLOCK) kb_trace_flat(BatchArgs A) {
     }
 }
 
+// kb_trace over the 4-wide layout, shaped as the single-scene persistent
+// walk (k_trace4_persistent): a lane keeps only its ray, its job and its
+// item, finds the job by a fresh binary search when it takes a ray, and
+// reads the job's tree from the job table at each step instead of holding
+// a copy, so the kernel fits the registers of 7 blocks of 128 per SM.
+// Idle lanes take new rays once `refill` of them are idle.  Each ray's walk
+// is the same as in the other stage kernels, so are the results.
+template <int BLOCK, bool SHADOW, int S1, int S2, int MODE>
+__global__ void __launch_bounds__(BLOCK, 896 / BLOCK) kb_trace4_refill(BatchArgs A) {
+    extern __shared__ uint2 smem_stack[];
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t nj = A.hdr->n_jobs;
+    const uint32_t n =
+        SHADOW ? *(volatile uint32_t*)(A.counters + kCtrShadowCount) : (uint32_t)A.hdr->rays;  // < 2^32 (launch)
+    uint32_t* counter = A.counters + (SHADOW ? kCtrShadowWork : kCtrExtendWork);
+    const uint32_t refill = SHADOW ? A.refill_shadow : A.refill;
+    constexpr uint32_t kNone = 0xffffffffu;
+    uint32_t next = 0, end = 0;
+    bool more = true;
+    uint32_t job = kNone, item = 0;
+    bool any = MODE == kAny;
+    DRay r;
+    Traversal4<S1, S2> T;
+    T.bind(smem_stack, threadIdx.x, blockDim.x);
+    auto finish = [&]() {
+        const JobRec& J = A.jobs[job];
+        if (T.overflow) atomicMax((int*)(J.P.counters + 2), 6);
+        if (SHADOW) {
+            J.P.occluded[__ldg(A.q_slot + item)] = T.found ? 1 : 0;
+        } else if (any) {
+            J.occ[item] = T.found ? 1 : 0;
+        } else if (T.nan_hit) {  // rewritten by the replay stage
+            J.hits[item] = make_float4(__int_as_float(kReplayMark), 0.0f, 0.0f, 0.0f);
+            A.counters[kCtrReplay] = 1u;
+        } else {
+            J.hits[item] = make_float4(__int_as_float(T.res.prim), T.res.t, T.res.b1, T.res.b2);
+        }
+        job = kNone;
+    };
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, job == kNone);
+        const unsigned nidle = __popc(idle);
+        if (more && next >= end && nidle >= refill) {  // warp-uniform
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(counter, A.chunk);
+            base = __shfl_sync(kFull, base, 0);
+            if (base < n) {
+                next = base;
+                end = n - base > A.chunk ? base + A.chunk : n;
+            } else {
+                more = false;
+            }
+        }
+        const bool tail = !more && next + nidle >= end;
+        if (next < end && nidle >= (tail ? 1u : refill)) {
+            if (job == kNone) {
+                const uint32_t my = next + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (my < end) {
+                    const float4* src;
+                    if (SHADOW) {
+                        job = __ldg(A.q_job + my);
+                        item = my;
+                        src = reinterpret_cast<const float4*>(A.q_rays) + 2 * (size_t)my;
+                    } else {
+                        Cursor c{0, 1, 0};
+                        job = locate(A.off_ray, nj, my, c);
+                        item = (uint32_t)(my - c.lo);
+                        if (MODE == kPerJob) any = A.jobs[job].any != 0;
+                        src = A.jobs[job].rays + 2 * (size_t)item;
+                    }
+                    r = make_dray(__ldg(src), __ldg(src + 1));
+                    if (!T.start(A.jobs[job].P.bvh4, r)) finish();
+                }
+            }
+            next += nidle;
+        }
+        if (!__any_sync(kFull, job != kNone)) {
+            if (next >= end && !more) break;
+            continue;
+        }
+        if (job != kNone) {
+            const DevBVH4& bv = A.jobs[job].P.bvh4;
+            bool going;
+            if (MODE == kClosest)
+                going = T.template step<false>(bv, r);
+            else if (MODE == kAny)
+                going = T.template step<true>(bv, r);
+            else
+                going = any ? T.template step<true>(bv, r) : T.template step<false>(bv, r);
+            if (!going) finish();
+        }
+    }
+}
+
 // The exact replay of the closest hits the extend stage marked (see
 // Traversal in trace.cuh): the binary walk with instances allowed; returns
 // at once when nothing was marked.
@@ -297,7 +391,15 @@ template <int BLOCK, bool SHADOW, bool WIDE, int S1, int S2, int MODE, bool FLAT
 cudaError_t go(const BatchArgs& A, int sms, cudaStream_t s) {
     static ShapeCache bps_cache;
     const size_t smem = WIDE ? (size_t)S1 * sizeof(uint2) * BLOCK : 0;
-    auto kernel = FLAT ? kb_trace_flat<BLOCK, SHADOW, WIDE, S1, S2, MODE> : kb_trace<BLOCK, SHADOW, WIDE, S1, S2, MODE>;
+    auto pick_kernel = [] {
+        if constexpr (FLAT)
+            return kb_trace_flat<BLOCK, SHADOW, WIDE, S1, S2, MODE>;
+        else if constexpr (WIDE)
+            return kb_trace4_refill<BLOCK, SHADOW, S1, S2, MODE>;
+        else
+            return kb_trace<BLOCK, SHADOW, WIDE, S1, S2, MODE>;
+    };
+    auto kernel = pick_kernel();
     const int bps = resident_blocks(bps_cache, kernel, BLOCK, smem);
     kernel<<<(unsigned)(sms * bps), BLOCK, smem, s>>>(A);
     return cudaGetLastError();

@@ -115,7 +115,10 @@ struct PbrtBatch {
     std::vector<Copy> h2d, d2h;  // staged host inputs / outputs of the jobs
     bool in_flight = false;
 
-    BatchTuning tune{1, 1, 128, 16, 64, 32, 32};  // 4-wide walks where every job has the layout
+    // 4-wide walks where every job has the layout; camera and query rays
+    // walked to the end per lane, shadow rays refilled once 8 lanes are idle
+    // (serving mix of 32 soups: 5280 against 5100 requests/s with 32 / 32)
+    BatchTuning tune{1, 1, 128, 16, 64, 32, 8};
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
     BatchTuning graph_tune{};

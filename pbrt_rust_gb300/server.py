@@ -34,7 +34,7 @@ class GpuServer:
             cfg.use_tuning = 1
             t = abi.PbrtBatchTuning()
             base = dict(extend_kernel="wide", shadow_kernel="wide", block=128, stack=16, chunk=64, refill=32,
-                        refill_shadow=32, use_graph=1)
+                        refill_shadow=8, use_graph=1)
             base.update(tuning)
             for k, v in base.items():
                 setattr(t, k, _KERNEL[v] if k in ("extend_kernel", "shadow_kernel") else int(v))
