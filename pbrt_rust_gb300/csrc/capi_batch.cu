@@ -383,6 +383,8 @@ int pbrtgpu_batch_add_render(PbrtBatch* b, const PbrtScene* cS, const PbrtCamera
         b->n_tasks + tasks.size() > L.max_tasks)
         return set_error(PBRT_ERR_BUDGET, "the render does not fit the batch's remaining jobs, samples, light "
                                           "samples, film pixels or tasks");
+    if (b->n_ray + P.n_samples >= (1ull << 31))  // the traversal stages count rays in 32 bits
+        return set_error(PBRT_ERR_BUDGET, "the batch's rays would reach 2^31");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(P.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
     const bool inst = P.bvh.insts != nullptr;  // batches walk instanced jobs over the binary layout
@@ -452,6 +454,10 @@ int pbrtgpu_batch_add_query(PbrtBatch* b, const PbrtBVH* cb, const PbrtRay* rays
     const PbrtBatchLimits& L = b->lim;
     if (b->n_jobs + 1 > L.max_jobs || (staged && b->n_stage + n > L.max_query_rays))
         return set_error(PBRT_ERR_BUDGET, "the query does not fit the batch's remaining jobs or staged rays");
+    // the traversal stages count the batch's rays in 32 bits (their work
+    // counters, the refilling walk's ray positions)
+    if (b->n_ray + n >= (1ull << 31))
+        return set_error(PBRT_ERR_BUDGET, "the batch's rays would reach 2^31");
     const uint32_t cp = (uint32_t)trace_stack_for_depth(B->host.depth);
     if (cp == 0) return set_error(PBRT_ERR_UNSUPPORTED, "BVH deeper than the batch kernels' stacks");
     const bool inst = B->dev.insts != nullptr;  // batches walk instanced jobs over the binary layout
